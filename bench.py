@@ -1,0 +1,452 @@
+"""Benchmark: einsum TFLOP/s on the CCD W intermediates (o=32, v=160), split-BF16
+vs plain FP64, with the error of every result against FP64 and a sampled
+CPU-oracle check.
+
+One step = the four contractions of the CCD configuration on one GPU:
+    Wmnij += 0.25 t_ijef g_mnef      (GEMM)
+    Wabef += 0.25 g_mnef t_mnab      (GEMM; Wabef is 25600 x 25600, 5.24 GB)
+    Wmbej += -0.5 t_jnfb g_mnef      (GENERIC)
+    E      = 0.25 sum t_ijab g_ijab  (DOT, always FP64)
+``value`` is the algorithmic FLOP count of a step (2*|C|*|links| per
+contraction) divided by the device time of the step, for the headline
+precision (split-BF16 when built, else FP64).  Inputs are larger than L2
+(129 MB), so no flush is needed between steps.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun (N > 1) each rank runs an independent replica (the path has no
+exchange step); value sums the replicas' work over the max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+O_DEF, V_DEF = 32, 160
+METRIC = "einsum TFLOP/s, split-BF16 vs plain FP64 at <=1e-10 rel err; % of roofline"
+
+
+def flops(o, v):
+    return {"Wmnij": 2.0 * o ** 4 * v ** 2, "Wabef": 2.0 * v ** 4 * o ** 2, "Wmbej": 2.0 * o ** 3 * v ** 3,
+            "E": 2.0 * o ** 2 * v ** 2}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p, "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    """Samples nvidia-smi during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            parts = [p.strip() for p in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------- our arm --
+def ccd_step(eg, T, W, precision, slices, timers=None):
+    """The four contractions; returns nothing (results stay on the device)."""
+    import torch
+    t, g = T["t"], T["g_oovv"]
+
+    def run(name, fn):
+        if timers is not None:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            timers.setdefault(name, []).append((e0, e1))
+        else:
+            fn()
+
+    run("Wmnij", lambda: eg.einsum(1.0, "mnij", W["Wmnij"], 0.25, "ijef", t, "mnef", g, precision=precision,
+                                   slices=slices))
+    run("Wabef", lambda: eg.einsum(1.0, "abef", W["Wabef"], 0.25, "mnef", g, "mnab", t, precision=precision,
+                                   slices=slices))
+    run("Wmbej", lambda: eg.einsum(1.0, "mbej", W["Wmbej"], -0.5, "jnfb", t, "mnef", g, precision=precision,
+                                   slices=slices))
+    run("E", lambda: eg.einsum(0.0, "", W["E"], 0.25, "ijab", t, "ijab", g))
+
+
+def fresh_W(T):
+    import torch
+    return {"Wmnij": T["g_oooo"].clone(), "Wabef": T["g_vvvv"].clone(), "Wmbej": T["g_ovvo"].clone(),
+            "E": torch.zeros((), dtype=torch.float64, device="cuda")}
+
+
+def rel_err(x, ref):
+    import torch
+    num = torch.linalg.vector_norm((x - ref).reshape(-1))
+    den = torch.linalg.vector_norm(ref.reshape(-1))
+    return float(num / den) if float(den) > 0 else float(num)
+
+
+def oracle_sample_check(T, W_fp64, o, v, rows=2):
+    """CPU-oracle values of a few rows of each W, against the GPU FP64 results."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    t = T["t"].cpu().numpy()
+    g = T["g_oovv"].cpu().numpy()
+    out = {}
+    ref = T["g_oooo"][:rows].cpu().numpy().copy()
+    oracle.einsum("mnij", ref, 1.0, 0.25, "ijef", t, "mnef", np.ascontiguousarray(g[:rows]))
+    out["Wmnij"] = oracle.rel_fro(W_fp64["Wmnij"][:rows].cpu().numpy(), ref)
+    ref = T["g_vvvv"][:rows].cpu().numpy().copy()
+    oracle.einsum("abef", ref, 1.0, 0.25, "mnef", g, "mnab", np.ascontiguousarray(t[:, :, :rows]))
+    out["Wabef"] = oracle.rel_fro(W_fp64["Wabef"][:rows].cpu().numpy(), ref)
+    ref = T["g_ovvo"][:rows].cpu().numpy().copy()
+    oracle.einsum("mbej", ref, 1.0, -0.5, "jnfb", t, "mnef", np.ascontiguousarray(g[:rows]))
+    out["Wmbej"] = oracle.rel_fro(W_fp64["Wmbej"][:rows].cpu().numpy(), ref)
+    e = np.zeros(())
+    oracle.einsum("", e, 0.0, 0.25, "ijab", t, "ijab", g)
+    out["E"] = abs(float(W_fp64["E"].item()) - float(e)) / max(abs(float(e)), 1e-300)
+    return out
+
+
+def cpu_sample(o, v, seed=0, frac_rows=None, threads=None):
+    """The oracle's CCD step on a bounded sample (slabs of the leading output
+    index); returns (seconds, algorithmic flops of the sample, description)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from einsums_gb300 import workloads
+    T = workloads.ccd_inputs(o, v, seed=seed, backend="numpy", with_vvvv=False)
+    t, g = T["t"], T["g_oovv"]
+    a_rows = frac_rows or max(1, v // 32)
+    m_rows = max(1, o // 16)
+    W1 = np.zeros((m_rows, o, o, o))
+    W2 = np.zeros((a_rows, v, v, v))
+    W3 = np.zeros((m_rows, v, v, o))
+    E = np.zeros(())
+    g_m = np.ascontiguousarray(g[:m_rows])
+    t_a = np.ascontiguousarray(t[:, :, :a_rows])
+    t0 = time.perf_counter()
+    oracle.einsum("mnij", W1, 1.0, 0.25, "ijef", t, "mnef", g_m)
+    oracle.einsum("abef", W2, 1.0, 0.25, "mnef", g, "mnab", t_a)
+    oracle.einsum("mbej", W3, 1.0, -0.5, "jnfb", t, "mnef", g_m)
+    oracle.einsum("", E, 0.0, 0.25, "ijab", t, "ijab", g)
+    dt = time.perf_counter() - t0
+    f = flops(o, v)
+    fl = f["Wmnij"] * m_rows / o + f["Wabef"] * a_rows / v + f["Wmbej"] * m_rows / o + f["E"]
+    desc = (f"oracle CCD step on slabs: Wmnij/Wmbej rows m<{m_rows} of {o}, Wabef rows a<{a_rows} of {v}, "
+            f"full E; numpy OpenBLAS dgemm + OpenMP generic loop")
+    return dt, fl, desc
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    import einsums_gb300 as eg
+    from einsums_gb300 import _lib, core, workloads
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    lib = _lib.load()
+    o, v = args.o, args.v
+    F = flops(o, v)
+    step_flops = sum(F.values())
+
+    # FP64 roofline denominator, measured on this device.
+    import ctypes
+    dfma, dmma = ctypes.c_double(), ctypes.c_double()
+    _lib.check(lib.eg_measure_fp64_peak(ctypes.byref(dfma), ctypes.byref(dmma)))
+    fp64_peak = max(dfma.value, dmma.value)
+
+    T = workloads.ccd_inputs(o, v, seed=args.seed, backend="cuda")
+    torch.cuda.synchronize()
+
+    # Which precision is the headline: split-BF16 when the library has it.
+    headline = "split_bf16"
+    try:
+        Wt = fresh_W(T)
+        ccd_step(eg, T, Wt, "split_bf16", args.slices)
+        torch.cuda.synchronize()
+        del Wt
+    except _lib.NotSupportedError:
+        headline = "fp64"
+
+    # Accuracy: one step each precision from the same initial W.
+    W64 = fresh_W(T)
+    ccd_step(eg, T, W64, "fp64", 0)
+    errors = {}
+    split_report = None
+    if headline == "split_bf16":
+        Ws = fresh_W(T)
+        ccd_step(eg, T, Ws, "split_bf16", args.slices)
+        split_report = core.last_split_report()
+        for k in ("Wmnij", "Wabef", "Wmbej"):
+            errors[k] = rel_err(Ws[k] - T[{"Wmnij": "g_oooo", "Wabef": "g_vvvv", "Wmbej": "g_ovvo"}[k]],
+                                W64[k] - T[{"Wmnij": "g_oooo", "Wabef": "g_vvvv", "Wmbej": "g_ovvo"}[k]])
+        del Ws
+    torch.cuda.synchronize()
+    oracle_err = oracle_sample_check(T, W64, o, v) if rank == 0 else None
+
+    def timed(precision, steps, warmup, timers=None):
+        W = fresh_W(T)
+        for _ in range(warmup):
+            ccd_step(eg, T, W, precision, args.slices)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        n0 = ctypes.c_uint64()
+        _lib.check(lib.eg_kernel_launches(ctypes.byref(n0)))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            ccd_step(eg, T, W, precision, args.slices, timers)
+        e1.record()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        n1 = ctypes.c_uint64()
+        _lib.check(lib.eg_kernel_launches(ctypes.byref(n1)))
+        del W
+        return e0.elapsed_time(e1) / steps, int(n1.value - n0.value)
+
+    # Plain FP64 reference timing (fewer steps: it is ~100x slower).
+    fp64_steps = 1 if headline == "split_bf16" else args.steps
+    fp64_timers = {}
+    ms_fp64, _ = timed("fp64", fp64_steps, 1, fp64_timers)
+
+    timers = {}
+    gpu_idx = int(os.environ.get("LOCAL_RANK", 0))
+    lib.eg_profile_enable(1)
+    lib.eg_profile_reset()
+    with ClockSampler(gpu_idx) as clk:
+        ms, launches = timed(headline, args.steps, args.warmup, timers)
+    buf = ctypes.create_string_buffer(1 << 16)
+    _lib.check(lib.eg_profile_summary(buf, len(buf)))
+    lib.eg_profile_enable(0)
+    kernels = {}
+    for line in buf.value.decode().strip().split("\n"):
+        if line:
+            name, cnt, tot = line.split(",")
+            kernels[name] = {"launches": int(cnt), "total_ms": float(tot)}
+
+    if world > 1:
+        t_ms = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t_ms, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t_ms.item())
+
+    per_contraction = {k: sum(a.elapsed_time(b) for a, b in vals) / len(vals) for k, vals in timers.items()}
+    per_contraction_fp64 = {k: sum(a.elapsed_time(b) for a, b in vals) / len(vals) for k, vals in fp64_timers.items()}
+    value = world * step_flops / (ms * 1e-3) / 1e12
+    fp64_value = step_flops / (ms_fp64 * 1e-3) / 1e12
+
+    # Dominant kernel roofline.
+    pk, pk_kind = peaks()
+    if headline == "split_bf16":
+        dom = max((k for k in kernels if k.startswith("k_tc")), key=lambda k: kernels[k]["total_ms"], default=None)
+    else:
+        dom = "k_contract_f64" if "k_contract_f64" in kernels else max(kernels, key=lambda k: kernels[k]["total_ms"])
+    roof = None
+    if dom:
+        d = kernels[dom]
+        avg_ms = d["total_ms"] / d["launches"]
+        if headline == "split_bf16":
+            pairs = (split_report or {}).get("slice_pairs", 0)
+            # bf16 flops issued by the tensor kernel per step (slice pairs x 2MNK over the GEMM-shaped W's)
+            alg = pairs * (F["Wmnij"] + F["Wabef"] + F["Wmbej"]) / (d["launches"] / args.steps)
+            ach = alg / (avg_ms * 1e-3) / 1e12
+            peak = pk.get("bf16_tflops_sustained", 1700.0)
+            roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                    "frac": ach / peak, "traffic": None, "peak_source": f"bf16 sustained, {pk_kind}"}
+        else:
+            alg = F["Wabef"]
+            ach = alg / (per_contraction["Wabef"] * 1e-3) / 1e12
+            roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
+                    "frac": ach / fp64_peak, "traffic": None,
+                    "peak_source": "fp64 measured live (max of DFMA and DMMA probes)"}
+
+    # End to end through the public API: host inputs in, host results out.
+    e2e = None
+    if rank == 0:
+        e2e = run_e2e(eg, T, headline, args, o, v, step_flops)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        dt, fl, desc = cpu_sample(o, v, seed=args.seed)
+        cpu = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": host_cores(), "kind": "port", "sample": desc,
+               "seconds": dt}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (split into bf16 slices, fp32 tensor accumulate)"
+            if headline == "split_bf16" else "f64",
+            "data": "synthetic (seeded torch generator on device; CCD amplitudes/integrals as specified)",
+            "config": {"workload": f"CCD W intermediates o={o} v={v}: Wmnij, Wabef (GEMM), Wmbej (GENERIC), E (DOT)",
+                       "precision": headline, "slices": (split_report or {}).get("slices"),
+                       "l2": "inputs larger than L2 (Wabef 5.24 GB read+written per step); no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "plain_fp64": {"value": fp64_value, "ms_per_step": ms_fp64, "per_contraction_ms": per_contraction_fp64,
+                           "fp64_peak_tflops": fp64_peak, "dfma_tflops": dfma.value, "dmma_tflops": dmma.value},
+            "split_vs_fp64_speedup": value / world / fp64_value if headline == "split_bf16" else None,
+            "per_contraction_ms": per_contraction, "kernels": kernels,
+            "error_vs_fp64": errors, "error_fp64_vs_oracle_sample": oracle_err, "split_report": split_report,
+            "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches,
+        }
+        print(json.dumps(line))
+
+
+def run_e2e(eg, T, precision, args, o, v, step_flops):
+    """Same step through the public API with host buffers: pinned host inputs are
+    copied in, and all four results are copied back, inside the timed region."""
+    import torch
+    host = {k: T[k].cpu().pin_memory() for k in ("t", "g_oovv", "g_oooo", "g_vvvv", "g_ovvo")}
+    out = {"Wmnij": torch.empty_like(host["g_oooo"]).pin_memory(),
+           "Wabef": torch.empty_like(host["g_vvvv"]).pin_memory(),
+           "Wmbej": torch.empty_like(host["g_ovvo"]).pin_memory(),
+           "E": torch.empty((), dtype=torch.float64).pin_memory()}
+    dev = {k: torch.empty_like(T[k]) for k in host}
+    W = {"Wmnij": dev["g_oooo"], "Wabef": dev["g_vvvv"], "Wmbej": dev["g_ovvo"],
+         "E": torch.zeros((), dtype=torch.float64, device="cuda")}
+    h2d = sum(x.numel() * 8 for x in host.values())
+    d2h = sum(x.numel() * 8 for x in out.values())
+
+    def step():
+        for k in host:
+            dev[k].copy_(host[k], non_blocking=True)
+        ccd_step(eg, {"t": dev["t"], "g_oovv": dev["g_oovv"]}, W, precision, args.slices)
+        for k in out:
+            out[k].copy_(W[k], non_blocking=True)
+
+    steps = max(1, min(args.steps, 3)) if precision == "fp64" else args.steps
+    for _ in range(max(1, args.warmup if precision != "fp64" else 1)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": step_flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": ms, "steps": steps}
+
+
+# --------------------------------------------------------- reference arm --
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    o, v = args.o, args.v
+    for _ in range(args.warmup):
+        cpu_sample(o, v, seed=args.seed)
+    times, fl, desc = [], 0.0, ""
+    for _ in range(args.steps):
+        dt, fl, desc = cpu_sample(o, v, seed=args.seed)
+        times.append(dt)
+    dt = sum(times) / len(times)
+    val = fl / dt / 1e12
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (numpy PCG64, seeded)",
+        "config": {"workload": f"CCD W intermediates o={o} v={v}: Wmnij, Wabef (GEMM), Wmbej (GENERIC), E (DOT)",
+                   "precision": "fp64 (reference CPU einsum restated: OpenBLAS dgemm + OpenMP generic loop)"},
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": host_cores(), "kind": "port", "sample": desc},
+        "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--o", type=int, default=O_DEF)
+    ap.add_argument("--v", type=int, default=V_DEF)
+    ap.add_argument("--slices", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world)
+    finally:
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

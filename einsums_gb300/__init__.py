@@ -1,0 +1,12 @@
+"""einsums_gb300: GB300-native (sm_103a) tensor-contraction hot path of Einsums.
+
+The product is the C-ABI library ``libeinsums_gb300.so`` (include/einsums_gb300.h);
+this package is its Python front end (``core``) plus the autograd binding.
+Importing it loads the CUDA library; there is no CPU fallback.
+"""
+from . import _lib
+from .core import (ALGORITHMS, EinsumDirectProductPlan, EinsumDotPlan, EinsumGemmPlan, EinsumGemvPlan,
+                   EinsumGenericPlan, EinsumGerPlan, compile_plan, einsum, last_split_report, permute)
+
+__all__ = ["compile_plan", "einsum", "permute", "last_split_report", "ALGORITHMS", "EinsumGenericPlan",
+           "EinsumDotPlan", "EinsumDirectProductPlan", "EinsumGerPlan", "EinsumGemvPlan", "EinsumGemmPlan"]

@@ -1,0 +1,209 @@
+"""Python front end mirroring the reference's EinsumsPy ``core`` module.
+
+``compile_plan(C, A, B)`` returns a plan object of the same class names as
+``libs/EinsumsPy/TensorAlgebra/src/Export.cpp:12-140`` and
+``plan.execute(C_prefactor, C, AB_prefactor, A, B)`` runs it, either on
+single tensors or on equal-length lists of tensors (the list overload).
+Operands are CUDA float64 ``torch.Tensor`` objects (any strides); all work
+goes through the C ABI of libeinsums_gb300.so on the current CUDA stream.
+
+``einsum`` / ``permute`` mirror the C++ ``einsum(C_prefactor, Indices{...},
+&C, AB_prefactor, Indices{...}, A, Indices{...}, B)`` and ``permute`` calls
+(with C++ semantics) for callers that name indices as strings or sequences.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Sequence
+
+import torch
+
+from . import _lib
+from ._lib import (PRECISION_FP64, PRECISION_SPLIT_BF16, SEMANTICS_CPP, SEMANTICS_PYTHON, EgOptions,
+                   EgSplitReport, EgTensor)
+
+ALGORITHMS = ["GENERIC", "DOT", "DIRECT", "GER", "GEMV", "GEMM", "INDETERMINATE"]
+
+
+def _tensor(t: torch.Tensor, name: str) -> EgTensor:
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name} must be a torch.Tensor")
+    if t.dtype != torch.float64:
+        raise TypeError(f"{name} must be float64 (got {t.dtype})")
+    if not t.is_cuda:
+        raise TypeError(f"{name} must live on a CUDA device")
+    if t.dim() > _lib.MAX_RANK:
+        raise _lib.RankError(2, f"{name} has rank {t.dim()} (max {_lib.MAX_RANK})")
+    e = EgTensor()
+    e.data = t.data_ptr() if t.numel() else None
+    e.rank = t.dim()
+    for i, (n, s) in enumerate(zip(t.shape, t.stride())):
+        e.extent[i] = n
+        e.stride[i] = s
+    return e
+
+
+def _options(precision: str, slices: int, semantics: int, only_generic: bool, tolerance: float) -> EgOptions:
+    o = EgOptions()
+    _lib.load().eg_options_default(ctypes.byref(o))
+    o.precision = {"fp64": PRECISION_FP64, "split_bf16": PRECISION_SPLIT_BF16}[precision]
+    o.slices = int(slices)
+    o.tolerance = float(tolerance)
+    o.semantics = semantics
+    o.only_generic = int(bool(only_generic))
+    return o
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        return torch.cuda.current_stream().cuda_stream
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+def _check_device(*ts):
+    dev = None
+    for t in ts:
+        if dev is None:
+            dev = t.device
+        elif t.device != dev:
+            raise ValueError("all operands must be on the same device")
+    if dev is not None and dev.index is not None and dev.index != torch.cuda.current_device():
+        raise ValueError("operands must be on the current CUDA device")
+
+
+def _run_einsum(C_prefactor, C_labels, C, AB_prefactor, A_labels, A, B_labels, B, *, semantics, precision="fp64",
+                slices=0, tolerance=1e-10, only_generic=False, stream=None) -> int:
+    lib = _lib.load()
+    if C.dim() != len(C_labels) or A.dim() != len(A_labels) or B.dim() != len(B_labels):
+        raise _lib.RankError(2, "tensor ranks do not match the indices")
+    _check_device(C, A, B)
+    ec, ea, eb = _tensor(C, "C"), _tensor(A, "A"), _tensor(B, "B")
+    opt = _options(precision, slices, semantics, only_generic, tolerance)
+    alg = ctypes.c_int32(-1)
+    _lib.check(lib.eg_einsum(float(C_prefactor), _lib.labels(C_labels), ctypes.byref(ec), float(AB_prefactor),
+                             _lib.labels(A_labels), ctypes.byref(ea), _lib.labels(B_labels), ctypes.byref(eb),
+                             ctypes.byref(opt), ctypes.c_void_p(_stream(stream)), ctypes.byref(alg)))
+    return alg.value
+
+
+def _run_batched(C_prefactor, C_labels, Cs, AB_prefactor, A_labels, As, B_labels, Bs, *, semantics,
+                 precision="fp64", slices=0, tolerance=1e-10, stream=None) -> int:
+    lib = _lib.load()
+    if not (len(Cs) == len(As) == len(Bs)):
+        raise ValueError("The lengths of the collections need to be the same!")
+    n = len(Cs)
+    if n == 0:
+        return -1
+    arrC, arrA, arrB = (EgTensor * n)(), (EgTensor * n)(), (EgTensor * n)()
+    for i in range(n):
+        if Cs[i].dim() != len(C_labels) or As[i].dim() != len(A_labels) or Bs[i].dim() != len(B_labels):
+            raise _lib.RankError(2, "tensor ranks do not match the indices")
+        _check_device(Cs[i], As[i], Bs[i])
+        arrC[i], arrA[i], arrB[i] = _tensor(Cs[i], "C"), _tensor(As[i], "A"), _tensor(Bs[i], "B")
+    opt = _options(precision, slices, semantics, False, tolerance)
+    alg = ctypes.c_int32(-1)
+    _lib.check(lib.eg_einsum_batched(float(C_prefactor), _lib.labels(C_labels), arrC, float(AB_prefactor),
+                                     _lib.labels(A_labels), arrA, _lib.labels(B_labels), arrB, n, ctypes.byref(opt),
+                                     ctypes.c_void_p(_stream(stream)), ctypes.byref(alg)))
+    return alg.value
+
+
+def classify(C_labels, A_labels, B_labels, semantics: int = SEMANTICS_CPP) -> int:
+    lib = _lib.load()
+    alg = ctypes.c_int32(-1)
+    _lib.check(lib.eg_classify(len(C_labels), _lib.labels(C_labels), len(A_labels), _lib.labels(A_labels),
+                               len(B_labels), _lib.labels(B_labels), semantics, ctypes.byref(alg)))
+    return alg.value
+
+
+# --------------------------------------------------------------- plans ----
+class EinsumGenericPlan:
+    """A compiled index pattern (``compile_plan`` result)."""
+
+    algorithm = "GENERIC"
+
+    def __init__(self, C: str, A: str, B: str):
+        self.C_indices, self.A_indices, self.B_indices = C, A, B
+
+    def execute(self, C_prefactor, C, AB_prefactor, A, B, *, precision: str = "fp64", slices: int = 0,
+                tolerance: float = 1e-10, stream=None):
+        """C = C_prefactor*C + AB_prefactor * A*B contracted over the plan's pattern.
+        ``C``, ``A``, ``B`` are tensors or equal-length lists of tensors."""
+        if isinstance(C, (list, tuple)):
+            _run_batched(C_prefactor, self.C_indices, list(C), AB_prefactor, self.A_indices, list(A),
+                         self.B_indices, list(B), semantics=SEMANTICS_PYTHON, precision=precision, slices=slices,
+                         tolerance=tolerance, stream=stream)
+            return
+        _run_einsum(C_prefactor, self.C_indices, C, AB_prefactor, self.A_indices, A, self.B_indices, B,
+                    semantics=SEMANTICS_PYTHON, precision=precision, slices=slices, tolerance=tolerance,
+                    stream=stream)
+
+    def __repr__(self):
+        return f"{type(self).__name__}({self.C_indices!r} <- {self.A_indices!r} * {self.B_indices!r})"
+
+
+class EinsumDotPlan(EinsumGenericPlan):
+    algorithm = "DOT"
+
+
+class EinsumDirectProductPlan(EinsumGenericPlan):
+    algorithm = "DIRECT"
+
+
+class EinsumGerPlan(EinsumGenericPlan):
+    algorithm = "GER"
+
+
+class EinsumGemvPlan(EinsumGenericPlan):
+    algorithm = "GEMV"
+
+
+class EinsumGemmPlan(EinsumGenericPlan):
+    algorithm = "GEMM"
+
+
+_PLAN_CLASSES = {0: EinsumGenericPlan, 1: EinsumDotPlan, 2: EinsumDirectProductPlan, 3: EinsumGerPlan,
+                 4: EinsumGemvPlan, 5: EinsumGemmPlan}
+
+
+def compile_plan(C_indices: str, A_indices: str, B_indices: str) -> EinsumGenericPlan:
+    """Pattern analysis of compile_plan (PyTensorAlgebra.cpp:168-554): returns the plan class
+    the reference returns for the same strings."""
+    alg = classify(C_indices, A_indices, B_indices, SEMANTICS_PYTHON)
+    return _PLAN_CLASSES[alg](C_indices, A_indices, B_indices)
+
+
+# ------------------------------------------------------ C++-style calls ----
+def einsum(C_prefactor, C_indices: Sequence, C, AB_prefactor, A_indices: Sequence, A, B_indices: Sequence, B, *,
+           precision: str = "fp64", slices: int = 0, tolerance: float = 1e-10, only_generic: bool = False,
+           stream=None) -> str:
+    """C++-semantics einsum; returns the reference's AlgorithmChoice name.  C, A, B may also
+    be equal-length lists (the batched overload)."""
+    if isinstance(C, (list, tuple)):
+        alg = _run_batched(C_prefactor, list(C_indices), list(C), AB_prefactor, list(A_indices), list(A),
+                           list(B_indices), list(B), semantics=SEMANTICS_CPP, precision=precision, slices=slices,
+                           tolerance=tolerance, stream=stream)
+        return ALGORITHMS[alg] if alg >= 0 else "INDETERMINATE"
+    alg = _run_einsum(C_prefactor, list(C_indices), C, AB_prefactor, list(A_indices), A, list(B_indices), B,
+                      semantics=SEMANTICS_CPP, precision=precision, slices=slices, tolerance=tolerance,
+                      only_generic=only_generic, stream=stream)
+    return ALGORITHMS[alg]
+
+
+def permute(C_prefactor, C_indices: Sequence, C, A_prefactor, A_indices: Sequence, A, *, stream=None) -> None:
+    """C = C_prefactor*C + A_prefactor*A[perm] (Permute.hpp:330-407)."""
+    lib = _lib.load()
+    C_indices, A_indices = list(C_indices), list(A_indices)
+    if C.dim() != len(C_indices) or A.dim() != len(A_indices):
+        raise _lib.RankError(2, "tensor ranks do not match the indices")
+    _check_device(C, A)
+    ec, ea = _tensor(C, "C"), _tensor(A, "A")
+    _lib.check(lib.eg_permute(float(C_prefactor), _lib.labels(C_indices), ctypes.byref(ec), float(A_prefactor),
+                              _lib.labels(A_indices), ctypes.byref(ea), ctypes.c_void_p(_stream(stream))))
+
+
+def last_split_report() -> dict:
+    r = EgSplitReport()
+    _lib.check(_lib.load().eg_last_split_report(ctypes.byref(r)))
+    return {"slices": r.slices, "slice_pairs": r.slice_pairs, "bits_per_slice": r.bits_per_slice,
+            "error_bound": r.error_bound}

@@ -1,0 +1,184 @@
+/*
+ * einsums_gb300 -- C ABI of the GB300 tensor-contraction library.
+ *
+ * Plain pointers and sizes only; no C++ or torch types cross this boundary.
+ * Every entry point returns an eg_status and never throws.  Tensors live in
+ * device memory owned by the caller; the library owns only its scratch
+ * workspace.  All work is ordered on the CUDA stream passed as `stream`
+ * (a cudaStream_t; NULL means the legacy default stream) and no entry point
+ * synchronises the host unless it is documented to return a host value.
+ *
+ * Each entry point names the reference interface it replaces (paths relative
+ * to the Einsums project root).
+ */
+#ifndef EINSUMS_GB300_H
+#define EINSUMS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EG_MAX_RANK 8
+
+typedef enum eg_status {
+    EG_SUCCESS = 0,
+    EG_ERROR_INVALID_ARGUMENT = 1, /* null pointer, bad option value */
+    EG_ERROR_RANK = 2,             /* rank_error: index count differs from tensor rank, or rank > EG_MAX_RANK */
+    EG_ERROR_DIMENSION = 3,        /* dimension_error: one index with two extents */
+    EG_ERROR_NOT_SUPPORTED = 4,    /* pattern or layout the kernels do not handle */
+    EG_ERROR_CUDA = 5,             /* a CUDA runtime call failed (eg_last_error has the text) */
+    EG_ERROR_OUT_OF_MEMORY = 6,    /* scratch allocation failed or exceeded the workspace budget */
+    EG_ERROR_TIMEOUT = 7,          /* a bounded device-side wait gave up; the context stays usable */
+    EG_ERROR_PRECISION = 8         /* split form cannot meet the requested tolerance */
+} eg_status;
+
+/* Same enumerators, same order as einsums::tensor_algebra::detail::AlgorithmChoice
+ * (libs/Einsums/TensorAlgebra/include/Einsums/TensorAlgebra/Detail/Utilities.hpp:26-34). */
+typedef enum eg_algorithm {
+    EG_ALGO_GENERIC = 0,
+    EG_ALGO_DOT = 1,
+    EG_ALGO_DIRECT = 2,
+    EG_ALGO_GER = 3,
+    EG_ALGO_GEMV = 4,
+    EG_ALGO_GEMM = 5,
+    EG_ALGO_INDETERMINATE = 6
+} eg_algorithm;
+
+typedef enum eg_precision {
+    EG_PRECISION_FP64 = 0,      /* plain FP64 kernels */
+    EG_PRECISION_SPLIT_BF16 = 1 /* FP64 operands split into exponent-scaled BF16 slices on tcgen05 */
+} eg_precision;
+
+typedef enum eg_semantics {
+    /* C++ einsum: an index found in only one operand and not in C is held at 0
+     * (Backends/BaseAlgebra.hpp:85-139); the DOT choice scales C by C_prefactor
+     * even when it is 0 (Backends/Dispatch.hpp:903-909). */
+    EG_SEMANTICS_CPP = 0,
+    /* EinsumsPy plans: every index of the unique-index space is summed and C is
+     * zeroed when C_prefactor == 0 (EinsumsPy/TensorAlgebra/PyTensorAlgebra.hpp:520-605). */
+    EG_SEMANTICS_PYTHON = 1
+} eg_semantics;
+
+/* A strided FP64 view of device memory; strides are in elements. */
+typedef struct eg_tensor {
+    double *data;
+    int32_t rank;
+    int64_t extent[EG_MAX_RANK];
+    int64_t stride[EG_MAX_RANK];
+} eg_tensor;
+
+typedef struct eg_options {
+    int32_t precision;    /* eg_precision */
+    int32_t slices;       /* split form: BF16 slices per operand, 2..8; 0 = chosen from `tolerance` */
+    double tolerance;     /* split form: target relative Frobenius error (default 1e-10) */
+    int32_t semantics;    /* eg_semantics */
+    int32_t only_generic; /* report and run as the generic algorithm (OnlyUseGenericAlgorithm) */
+} eg_options;
+
+/* Fills *opt with FP64 precision, automatic slices, tolerance 1e-10, C++ semantics. */
+void eg_options_default(eg_options *opt);
+
+/*
+ * C = C_prefactor * C + AB_prefactor * sum_links A * B
+ *
+ * Replaces einsums::tensor_algebra::einsum(C_prefactor, Indices{...}, &C, AB_prefactor,
+ * Indices{...}, A, Indices{...}, B, &algorithm_choice)
+ * (libs/Einsums/TensorAlgebra/include/Einsums/TensorAlgebra/TensorAlgebra.hpp:41-50,
+ *  implementation Backends/Dispatch.hpp:960-1262) for DeviceTensor operands, and the
+ * GPU branch of the EinsumsPy plans' execute
+ * (libs/EinsumsPy/TensorAlgebra/src/PyTensorAlgebra.cpp:609-1049).
+ * Labels: one int32 per mode; equal labels name the same index.  A rank-0 C is a
+ * single device double.  *algorithm_choice (may be NULL) receives the algorithm the
+ * reference reports for the same call.
+ */
+eg_status eg_einsum(double C_prefactor, const int32_t *C_labels, const eg_tensor *C, double AB_prefactor,
+                    const int32_t *A_labels, const eg_tensor *A, const int32_t *B_labels, const eg_tensor *B,
+                    const eg_options *opt, void *stream, int32_t *algorithm_choice);
+
+/*
+ * Algorithm choice of a pattern without running it (no stride vetoes).
+ * Replaces the dry-run dispatch detail::einsum<false, true, ...>
+ * (Backends/Dispatch.hpp:1276-1279) and compile_plan's plan-type selection
+ * (EinsumsPy/TensorAlgebra/src/PyTensorAlgebra.cpp:168-554).
+ */
+eg_status eg_classify(int32_t C_rank, const int32_t *C_labels, int32_t A_rank, const int32_t *A_labels, int32_t B_rank,
+                      const int32_t *B_labels, int32_t semantics, int32_t *algorithm_choice);
+
+/*
+ * C = C_prefactor * C + A_prefactor * A[perm]   (C zeroed first when C_prefactor == 0)
+ * Replaces einsums::tensor_algebra::permute(UC_prefactor, Indices{...}, &C, UA_prefactor,
+ * Indices{...}, A) (libs/Einsums/TensorAlgebra/include/Einsums/TensorAlgebra/Permute.hpp:330-407;
+ * device form Backends/DevicePermute.hpp:98-209).  Bit-exact copy when A_prefactor == 1
+ * and C_prefactor == 0.  EG_ERROR_DIMENSION when an extent of C is smaller than the
+ * matching extent of A.
+ */
+eg_status eg_permute(double C_prefactor, const int32_t *C_labels, const eg_tensor *C, double A_prefactor,
+                     const int32_t *A_labels, const eg_tensor *A, void *stream);
+
+/*
+ * List einsum: item i computes C[i] = C_prefactor*C[i] + AB_prefactor * A[i]*B[i] with one
+ * shared index pattern.  Items may have different extents.  Contractions that lower to a
+ * matrix product run as one persistent grouped launch over a device-side work list.
+ * Replaces the batched overload einsum(C_prefactor, Cidx, &C_list, AB_prefactor, Aidx,
+ * A_list, Bidx, B_list, &algorithm_choice) (Backends/Dispatch.hpp:1264-1286) and the list
+ * form of Plan.execute (EinsumsPy/TensorAlgebra/src/Export.cpp:17-27).
+ */
+eg_status eg_einsum_batched(double C_prefactor, const int32_t *C_labels, const eg_tensor *C_list, double AB_prefactor,
+                            const int32_t *A_labels, const eg_tensor *A_list, const int32_t *B_labels,
+                            const eg_tensor *B_list, int64_t count, const eg_options *opt, void *stream,
+                            int32_t *algorithm_choice);
+
+/* Split-form accounting for the last eg_einsum / eg_einsum_batched call on this host
+ * thread: slices used per operand, BF16 slice-pair products issued, and the a-priori
+ * relative error bound.  No reference counterpart (the reference has no split form). */
+typedef struct eg_split_report {
+    int32_t slices;
+    int32_t slice_pairs;
+    int32_t bits_per_slice;
+    double error_bound;
+} eg_split_report;
+eg_status eg_last_split_report(eg_split_report *out);
+
+/* Device storage for DeviceTensor (Tensor/include/Einsums/Tensor/Backends/DeviceTensor.hpp:246-284,
+ * GPUMemory/GPUAllocator.hpp:53-190): allocate / free device memory with an optional byte
+ * budget (0 = unlimited).  EG_ERROR_OUT_OF_MEMORY when the budget would be exceeded. */
+eg_status eg_device_alloc(size_t bytes, void **ptr);
+eg_status eg_device_free(void *ptr);
+eg_status eg_set_memory_budget(size_t bytes);
+eg_status eg_memory_in_use(size_t *bytes);
+
+/* Host<->device copies on `stream` (DeviceTensor::read / operator= in DeviceTensor.hpp). */
+eg_status eg_copy_to_device(void *dst, const void *src, size_t bytes, void *stream);
+eg_status eg_copy_to_host(void *dst, const void *src, size_t bytes, void *stream);
+eg_status eg_stream_synchronize(void *stream);
+
+/* Measures FP64 throughput of this device (TFLOP/s) with a DFMA loop and an
+ * mma.sync m8n8k4 f64 (DMMA) loop; synchronises the device.  The roofline
+ * denominator of the plain FP64 form.  No reference counterpart. */
+eg_status eg_measure_fp64_peak(double *dfma_tflops, double *dmma_tflops);
+
+/* Kernel accounting.  eg_kernel_launches: kernels this library has launched in the
+ * process.  With profiling on, every launch is bracketed by CUDA events on its own
+ * stream; eg_profile_summary synchronises those events and writes one line
+ * "name,launches,total_ms" per kernel into buf (NUL-terminated, truncated to cap).
+ * Replaces the scoped-zone profiler of the reference
+ * (libs/Einsums/Profile/include/Einsums/Profile/Profile.hpp:115-320) for the device path. */
+eg_status eg_kernel_launches(uint64_t *count);
+eg_status eg_profile_enable(int32_t on);
+eg_status eg_profile_reset(void);
+eg_status eg_profile_summary(char *buf, size_t cap);
+
+/* Text of the last error on this host thread (empty when none). */
+const char *eg_last_error(void);
+const char *eg_status_string(eg_status status);
+/* Library version string. */
+const char *eg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EINSUMS_GB300_H */

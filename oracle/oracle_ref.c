@@ -112,10 +112,10 @@ void oracle_generic_py(int n_unique, const int64_t *udims, const int64_t *sC, co
 }
 
 /* Element loop of permute (Permute.hpp:389-405): for every C index,
- * C[idx] = beta * C[idx] + alpha * A[perm(idx)].  beta == 0 has already
- * zeroed C in the caller (Permute.hpp:381-386); the expression is still
- * evaluated in full as the reference does.  sA_c[d] is the stride of A along
- * the A mode that carries C's d-th index. */
+ * C[idx] = beta * C[idx] + alpha * A[perm(idx)].  Basic tensors go through
+ * HPTT (Permute.hpp:375-378), whose beta == 0 path stores alpha * A without
+ * reading C; that is reproduced here, so -0.0 keeps its sign.  sA_c[d] is the
+ * stride of A along the A mode that carries C's d-th index. */
 void oracle_permute(int rank, const int64_t *cdims, const int64_t *sC, const int64_t *sA_c,
                     double beta, double *C, double alpha, const double *A) {
     int64_t idx[ORACLE_MAX_RANK] = {0};
@@ -124,8 +124,8 @@ void oracle_permute(int rank, const int64_t *cdims, const int64_t *sC, const int
     int64_t ic = 0, ia = 0;
     for (int64_t s = 0; s < total; s++) {
         double a = A[ia];
-        double t = C[ic];
-        C[ic] = beta * t + alpha * a;
+        /* HPTT's beta == 0 kernels write alpha * A without reading B. */
+        C[ic] = (beta == 0.0) ? alpha * a : beta * C[ic] + alpha * a;
         for (int d = rank - 1; d >= 0; d--) {
             idx[d]++;
             ic += sC[d];
