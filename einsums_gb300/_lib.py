@@ -87,6 +87,7 @@ PROTOTYPES = {
     "eg_copy_to_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "eg_copy_to_host": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     "eg_stream_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "eg_stream_status": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_int32)]),
     "eg_measure_fp64_peak": (ctypes.c_int, [_P(ctypes.c_double), _P(ctypes.c_double)]),
     "eg_kernel_launches": (ctypes.c_int, [_P(ctypes.c_uint64)]),
     "eg_profile_enable": (ctypes.c_int, [ctypes.c_int32]),

@@ -108,6 +108,24 @@ eg_status workspace(cudaStream_t stream, size_t bytes, void **ptr) {
 void set_split_report(const eg_split_report &r) { g_split_report = r; }
 
 namespace {
+std::mutex g_status_mutex;
+std::map<WsKey, int *> g_status;
+} // namespace
+
+eg_status status_word(cudaStream_t stream, int **ptr) {
+    int dev = 0;
+    EG_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_status_mutex);
+    int *&w = g_status[WsKey{dev, stream}];
+    if (!w) {
+        EG_CUDA(cudaMalloc(&w, 256));
+        EG_CUDA(cudaMemset(w, 0, 256));
+    }
+    *ptr = w;
+    return EG_SUCCESS;
+}
+
+namespace {
 
 using detail::Algorithm;
 using detail::Labels;
@@ -442,6 +460,20 @@ eg_status eg_copy_to_host(void *dst, const void *src, size_t bytes, void *stream
 
 eg_status eg_stream_synchronize(void *stream) {
     EG_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return EG_SUCCESS;
+}
+
+eg_status eg_stream_status(void *stream, int32_t *device_code) {
+    eg::set_error("");
+    int *w = nullptr;
+    eg_status st = eg::status_word((cudaStream_t)stream, &w);
+    if (st != EG_SUCCESS) return st;
+    EG_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    int code = 0;
+    EG_CUDA(cudaMemcpy(&code, w, sizeof(int), cudaMemcpyDeviceToHost));
+    if (code) EG_CUDA(cudaMemset(w, 0, sizeof(int)));
+    if (device_code) *device_code = code;
+    if (code) return eg::fail(EG_ERROR_TIMEOUT, "a bounded device wait gave up (code " + std::to_string(code) + ")");
     return EG_SUCCESS;
 }
 

@@ -90,6 +90,11 @@ struct Contraction {
 // library is loaded.  Calls that share a stream are ordered, so reuse is safe.
 eg_status workspace(cudaStream_t stream, size_t bytes, void **ptr);
 
+// Device-side error word of kernels with bounded waits, one per (device,
+// stream); kernels set it with atomicCAS(ptr, 0, code) and eg_stream_status
+// reads and clears it.
+eg_status status_word(cudaStream_t stream, int **ptr);
+
 // Device memory accounting used by eg_device_alloc and the workspace.
 eg_status tracked_malloc(size_t bytes, void **ptr);
 eg_status tracked_free(void *ptr);

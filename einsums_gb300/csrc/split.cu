@@ -1,0 +1,324 @@
+// Host orchestration of the split-BF16 form and its digit-splitting kernels.
+//
+//   k_split_rowmax   max |x| of every operand row (atomicMax on the bit
+//                    pattern of |x|, which orders like the value; deterministic)
+//   k_split_exponent row exponent e with |x| < 2^e (INT_MIN for a row holding
+//                    Inf/NaN, whose outputs are written as NaN)
+//   k_split_digits   32x32 tiles staged through shared memory so the operand is
+//                    read along its contiguous mode and the digit planes are
+//                    written along k; padding rows/columns are written as 0
+// then the tcgen05 GEMM (tc_gemm.cu) over the digit planes.  The operands'
+// index permutation is folded into the address maps of these kernels and of
+// the GEMM epilogue: nothing but the BF16 digit planes is materialised.
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include "split.cuh"
+
+namespace eg {
+void set_split_report(const eg_split_report &r);
+}
+
+namespace eg::split {
+
+namespace {
+
+// Operand view for the splitting kernels: rows (batch x row group) and k.
+struct OperandMap {
+    ModeGroup bg, rg, kg;
+    int comp;          // stride component: 0 for A, 1 for B
+    int64_t rows, Rp;  // logical and padded rows per batch
+    int64_t K, Kp;
+    int nbatch;
+};
+
+__device__ __forceinline__ int64_t comp_of(int comp, int64_t oa, int64_t ob) { return comp == 0 ? oa : ob; }
+
+__device__ __forceinline__ int64_t off_b(const OperandMap &m, int64_t b) {
+    int64_t oa, ob, oc;
+    group_offsets(m.bg, b, oa, ob, oc);
+    return comp_of(m.comp, oa, ob);
+}
+__device__ __forceinline__ int64_t off_r(const OperandMap &m, int64_t r) {
+    int64_t oa, ob, oc;
+    group_offsets32(m.rg, (uint32_t)r, oa, ob, oc);
+    return comp_of(m.comp, oa, ob);
+}
+__device__ __forceinline__ int64_t off_k(const OperandMap &m, int64_t k) {
+    int64_t oa, ob, oc;
+    group_offsets32(m.kg, (uint32_t)k, oa, ob, oc);
+    return comp_of(m.comp, oa, ob);
+}
+
+constexpr int T = 32, TR = 8;
+
+// Tiles of 32 rows x 32 k; row_fast: the operand is contiguous along rows.
+__global__ void __launch_bounds__(T *TR) k_split_rowmax(OperandMap m, const double *__restrict__ X,
+                                                        unsigned long long *rowmax, int row_fast) {
+    __shared__ unsigned long long red[TR][T];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int64_t rt = (m.rows + T - 1) / T, kt = (m.K + T - 1) / T;
+    const int64_t work = (int64_t)m.nbatch * rt * kt;
+    for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
+        const int64_t ktile = w % kt, rtile = (w / kt) % rt, b = w / (kt * rt);
+        const int64_t ob = off_b(m, b);
+        const int64_t r0 = rtile * T, k0 = ktile * T;
+        unsigned long long mx = 0;
+        if (row_fast) {
+            // thread (tx, ty): row r0+tx, k = k0+ty, +8, ...
+            const int64_t r = r0 + tx;
+            if (r < m.rows) {
+                const int64_t orow = ob + off_r(m, r);
+                for (int j = ty; j < T; j += TR) {
+                    const int64_t k = k0 + j;
+                    if (k < m.K) mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(X + orow + off_k(m, k)))));
+                }
+            }
+            red[ty][tx] = mx;
+            __syncthreads();
+            if (ty == 0) {
+                for (int j = 1; j < TR; j++) mx = max(mx, red[j][tx]);
+                if (r < m.rows && mx) atomicMax(rowmax + b * m.Rp + r, mx);
+            }
+            __syncthreads();
+        } else {
+            // thread (tx, ty): k = k0+tx, rows r0+ty, +8, ...; warp reduce along k
+            const int64_t k = k0 + tx;
+            const int64_t ok = k < m.K ? off_k(m, k) : 0;
+            for (int j = ty; j < T; j += TR) {
+                const int64_t r = r0 + j;
+                unsigned long long v = 0;
+                if (r < m.rows && k < m.K) v = (unsigned long long)__double_as_longlong(fabs(__ldg(X + ob + off_r(m, r) + ok)));
+                for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+                if (tx == 0 && r < m.rows && v) atomicMax(rowmax + b * m.Rp + r, v);
+            }
+        }
+    }
+}
+
+__global__ void k_split_exponent(const unsigned long long *rowmax, int *e, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double mx = __longlong_as_double((long long)rowmax[i]);
+        int ex = 0;
+        if (!isfinite(mx))
+            ex = INT_MIN;
+        else if (mx > 0.0)
+            frexp(mx, &ex); // mx = f 2^ex with f in [0.5, 1): |x| <= mx < 2^ex
+        e[i] = ex;
+    }
+}
+
+// Balanced base-256 digits of x * 2^(7 + 8(S-1) - e), least significant last.
+__device__ __forceinline__ void to_digits(double x, int e, int S, int *dig) {
+    const double y = scalbn(x, kTopBits + kBits * (S - 1) - e);
+    long long F = __double2ll_rn(y);
+    for (int s = S - 1; s >= 1; s--) {
+        int d = (int)(F & 255);
+        if (d > 128) d -= 256;
+        dig[s] = d;
+        F = (F - d) / 256;
+    }
+    dig[0] = (int)F;
+}
+
+__global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const double *__restrict__ X, const int *rexp,
+                                                        __nv_bfloat16 *planes, int S, int row_fast) {
+    __shared__ double tile[T][T + 1];
+    __shared__ int ex[T];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int64_t rt = m.Rp / T, kt = m.Kp / T;
+    const int64_t work = (int64_t)m.nbatch * rt * kt;
+    const int64_t plane = m.Rp * m.Kp;
+    for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
+        const int64_t ktile = w % kt, rtile = (w / kt) % rt, b = w / (kt * rt);
+        const int64_t ob = off_b(m, b);
+        const int64_t r0 = rtile * T, k0 = ktile * T;
+        if (ty == 0) ex[tx] = (r0 + tx < m.rows) ? rexp[b * m.Rp + r0 + tx] : 0;
+        if (row_fast) {
+            const int64_t r = r0 + tx;
+            const int64_t orow = r < m.rows ? ob + off_r(m, r) : 0;
+            for (int j = ty; j < T; j += TR) {
+                const int64_t k = k0 + j;
+                tile[tx][j] = (r < m.rows && k < m.K) ? __ldg(X + orow + off_k(m, k)) : 0.0;
+            }
+        } else {
+            const int64_t k = k0 + tx;
+            const int64_t okk = k < m.K ? off_k(m, k) : 0;
+            for (int j = ty; j < T; j += TR) {
+                const int64_t r = r0 + j;
+                tile[j][tx] = (r < m.rows && k < m.K) ? __ldg(X + ob + off_r(m, r) + okk) : 0.0;
+            }
+        }
+        __syncthreads();
+        // write: consecutive threads walk k in every digit plane
+        for (int j = ty; j < T; j += TR) {
+            const int64_t r = r0 + j;
+            int dig[kMaxSlices];
+            const int e = ex[j];
+            if (e == INT_MIN) {
+                for (int s = 0; s < S; s++) dig[s] = 0;
+            } else {
+                to_digits(tile[j][tx], e, S, dig);
+            }
+            __nv_bfloat16 *out = planes + ((int64_t)b * S) * plane + r * m.Kp + k0 + tx;
+            for (int s = 0; s < S; s++) out[(int64_t)s * plane] = __float2bfloat16_rn((float)dig[s]);
+        }
+        __syncthreads();
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    });
+    return fn;
+}
+
+// 3-D map over [planes][rows][Kp] BF16, box 64 (k) x 128 (rows) x 1, 128-byte swizzle.
+eg_status encode_planes(CUtensorMap *map, void *base, int64_t Kp, int64_t rows, int64_t planes) {
+    auto fn = encode_fn();
+    if (!fn) return fail(EG_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)planes};
+    cuuint64_t strides[2] = {(cuuint64_t)(Kp * 2), (cuuint64_t)(Kp * 2 * rows)};
+    cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)kBM, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(EG_ERROR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return EG_SUCCESS;
+}
+
+int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+bool is_fast(const ModeGroup &g, int comp) { return g.n > 0 && g.s[comp][g.n - 1] == 1; }
+
+eg_status split_operand(const OperandMap &om, const double *X, unsigned long long *rowmax, int *rexp,
+                        __nv_bfloat16 *planes, int S, cudaStream_t s) {
+    const bool k_fast = is_fast(om.kg, om.comp);
+    const bool r_fast = !k_fast && is_fast(om.rg, om.comp);
+    EG_CUDA(cudaMemsetAsync(rowmax, 0, (size_t)om.nbatch * om.Rp * sizeof(unsigned long long), s));
+    const int cap = num_sms() * 16;
+    {
+        const int64_t work = (int64_t)om.nbatch * ((om.rows + T - 1) / T) * ((om.K + T - 1) / T);
+        const int grid = (int)(work < cap ? (work < 1 ? 1 : work) : cap);
+        LaunchScope ls_("k_split_rowmax", s);
+        k_split_rowmax<<<grid, dim3(T, TR), 0, s>>>(om, X, rowmax, r_fast ? 1 : 0);
+    }
+    EG_CHECK_LAUNCH("k_split_rowmax");
+    {
+        const int64_t n = (int64_t)om.nbatch * om.Rp;
+        LaunchScope ls_("k_split_exponent", s);
+        k_split_exponent<<<(int)std::min<int64_t>((n + 255) / 256, cap), 256, 0, s>>>(rowmax, rexp, n);
+    }
+    EG_CHECK_LAUNCH("k_split_exponent");
+    {
+        const int64_t work = (int64_t)om.nbatch * (om.Rp / T) * (om.Kp / T);
+        const int grid = (int)(work < cap ? work : cap);
+        LaunchScope ls_("k_split_digits", s);
+        k_split_digits<<<grid, dim3(T, TR), 0, s>>>(om, X, rexp, planes, S, r_fast ? 1 : 0);
+    }
+    EG_CHECK_LAUNCH("k_split_digits");
+    return EG_SUCCESS;
+}
+
+} // namespace
+
+} // namespace eg::split
+
+namespace eg {
+
+eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s, eg_split_report *rep) {
+    using namespace split;
+    const int S = slices ? slices : 5;
+    if (S < 2 || S > kMaxSlices) return fail(EG_ERROR_INVALID_ARGUMENT, "split form: slices must be in 2..6");
+    const int64_t nb = c.batch.total, M = c.m.total, N = c.n.total, K = c.k.total;
+    if (M >= (int64_t(1) << 31) || N >= (int64_t(1) << 31) || K >= (int64_t(1) << 31) || nb * S >= (int64_t(1) << 31))
+        return fail(EG_ERROR_NOT_SUPPORTED, "split form: a mode group exceeds 2^31 elements");
+    const int64_t Kp = round_up(K, kBK), Mp = round_up(M, kBM), Np = round_up(N, kBN);
+
+    // workspace: digit planes of A and B, row maxima, exponents, status word
+    const size_t bytesA = (size_t)nb * S * Mp * Kp * 2, bytesB = (size_t)nb * S * Np * Kp * 2;
+    const size_t offB = round_up((int64_t)bytesA, 1024);
+    const size_t offMaxA = offB + round_up((int64_t)bytesB, 1024);
+    const size_t offMaxB = offMaxA + round_up(nb * Mp * 8, 256);
+    const size_t offEA = offMaxB + round_up(nb * Np * 8, 256);
+    const size_t offEB = offEA + round_up(nb * Mp * 4, 256);
+    const size_t total = offEB + round_up(nb * Np * 4, 256);
+    void *ws = nullptr;
+    eg_status st = workspace(s, total, &ws);
+    if (st != EG_SUCCESS) return st;
+    char *base = (char *)ws;
+    __nv_bfloat16 *planesA = (__nv_bfloat16 *)base, *planesB = (__nv_bfloat16 *)(base + offB);
+    unsigned long long *maxA = (unsigned long long *)(base + offMaxA), *maxB = (unsigned long long *)(base + offMaxB);
+    int *eA = (int *)(base + offEA), *eB = (int *)(base + offEB);
+    int *status = nullptr;
+    if ((st = status_word(s, &status)) != EG_SUCCESS) return st;
+
+    OperandMap oa{c.batch, c.m, c.k, 0, M, Mp, K, Kp, (int)nb};
+    OperandMap ob{c.batch, c.n, c.k, 1, N, Np, K, Kp, (int)nb};
+    if ((st = split_operand(oa, c.A, maxA, eA, planesA, S, s)) != EG_SUCCESS) return st;
+    if ((st = split_operand(ob, c.B, maxB, eB, planesB, S, s)) != EG_SUCCESS) return st;
+
+    CUtensorMap tmA, tmB;
+    if ((st = encode_planes(&tmA, planesA, Kp, Mp, nb * S)) != EG_SUCCESS) return st;
+    if ((st = encode_planes(&tmB, planesB, Kp, Np, nb * S)) != EG_SUCCESS) return st;
+
+    TcGemmParams p{};
+    p.S = S;
+    p.mtiles = (int)(Mp / kBM);
+    p.ntiles = (int)(Np / kBN);
+    p.nbatch = (int)nb;
+    p.M = M;
+    p.N = N;
+    p.Mp = (int)Mp;
+    p.Np = (int)Np;
+    p.bg = c.batch;
+    p.mg = c.m;
+    p.ng = c.n;
+    p.C = c.C;
+    p.ab = c.ab;
+    p.eA = eA;
+    p.eB = eB;
+    p.shift_const = -2 * kTopBits - kBits * (S - 1);
+    p.status = status;
+    p.timeout_ns = 2000ull * 1000 * 1000;
+
+    // K passes small enough for the exact int64 accumulator; later passes add into C.
+    const int64_t kpass = max_k_per_pass(S);
+    const int64_t nkb_total = Kp / kBK;
+    const int64_t kb_per_pass = kpass / kBK;
+    if (kb_per_pass < 1) return fail(EG_ERROR_NOT_SUPPORTED, "split form: slice count too large for exact accumulation");
+    for (int64_t kb0 = 0; kb0 < nkb_total || kb0 == 0; kb0 += kb_per_pass) {
+        p.kb0 = (int)kb0;
+        p.nkb = (int)std::min<int64_t>(kb_per_pass, nkb_total - kb0);
+        const bool first = kb0 == 0;
+        p.cp = first ? c.cp : 1.0;
+        p.zero = first ? (c.zero_when_cp_zero ? 1 : 0) : 0;
+        if (p.nkb <= 0) break;
+        if ((st = launch_tc_gemm(tmA, tmB, p, s)) != EG_SUCCESS) return st;
+    }
+    if (rep) {
+        rep->slices = S;
+        rep->slice_pairs = S * (S + 1) / 2;
+        rep->bits_per_slice = kBits;
+        rep->error_bound = error_bound(S);
+    }
+    return EG_SUCCESS;
+}
+
+} // namespace eg

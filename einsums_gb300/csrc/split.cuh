@@ -1,0 +1,73 @@
+// Split-BF16 ("Ozaki") form of the canonical contraction.
+//
+// Every FP64 operand row (a fixed (batch, m) of A, or (batch, n) of B, over
+// all summed modes k) is scaled by its own power of two 2^e, |x| < 2^e, and
+// cut into S balanced base-256 digits:
+//     x = 2^(e-7) * sum_{s<S} a_s 2^(-8 s),   a_s integer in [-128, 128]
+// so each digit ("slice") is exact in BF16 and a slice product is an integer
+// below 2^14.  The product of two rows is
+//     sum_k A B = 2^(eA+eB-14) * sum_d 2^(-8 d) G_d,   G_d = sum_{s+t=d} sum_k a_s b_t
+// and the triangular truncation keeps d < S (S(S+1)/2 slice pairs).  The
+// tensor cores accumulate G_d in FP32 over chunks of at most 1024 products,
+// which keeps every partial sum an integer of at most 2^24 and therefore
+// exact; the epilogue converts each chunk to an integer and accumulates
+//     R = sum_d 2^(8 (S-1-d)) G_d
+// exactly in int64 in tensor memory.  The only roundings of the whole
+// product are the digit truncation and the final int64 -> FP64 conversion.
+// This is the scheme of Ozaki, Ogita, Oishi and Rump (Numer. Algorithms 59,
+// 2012) as mapped to integer-exact tensor-core products by Ootomo, Ozaki and
+// Yokota (IJHPCA 2024), with BF16 digits and FP32 accumulation.
+#pragma once
+
+#include <cuda.h>
+
+#include "common.cuh"
+
+namespace eg::split {
+
+constexpr int kBits = 8;        // digit width
+constexpr int kTopBits = 7;     // magnitude bits of the leading digit
+constexpr int kMaxSlices = 6;   // keeps the scaled digits and the int64 accumulator in range
+constexpr int kBM = 128, kBN = 128, kBK = 64;
+constexpr int kChunkKB = 16;    // 16 x 64 = 1024 products per exact FP32 chunk
+
+struct TcGemmParams {
+    int S;
+    int nkb;  // K blocks in this pass
+    int kb0;  // first K block of this pass
+    int mtiles, ntiles, nbatch;
+    int64_t M, N;
+    int Mp, Np;
+    ModeGroup bg, mg, ng; // output offsets in C (component 2)
+    double *C;
+    double cp, ab;
+    int zero;
+    const int *eA; // [nbatch][Mp] row exponents; INT_MIN marks a non-finite row
+    const int *eB; // [nbatch][Np]
+    int shift_const; // -14 - 8 (S-1)
+    int *status;
+    unsigned long long timeout_ns;
+};
+
+eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p, cudaStream_t s);
+
+// Largest K (a multiple of kBK) one pass may sum without the int64 accumulator
+// overflowing 2^62 for S slices.
+inline int64_t max_k_per_pass(int S) {
+    // |R| <= K * 2^14 * sum_d (d+1) 2^(8 (S-1-d))
+    double w = 0.0;
+    for (int d = 0; d < S; d++) w += (d + 1) * std::ldexp(1.0, 8 * (S - 1 - d));
+    double kmax = std::ldexp(1.0, 62) / (std::ldexp(1.0, 14) * w);
+    int64_t k = (int64_t)kmax;
+    return (k / kBK) * kBK;
+}
+
+// A-priori bound on the relative error of one product, relative to
+// sum_k |A_row| |B_col| scaled to the row maxima: the dropped digit tail of
+// both operands plus the dropped cross terms with s + t >= S.
+inline double error_bound(int S) {
+    const double u = std::ldexp(1.0, -(kTopBits + kBits * (S - 1))); // one unit of the last digit, relative
+    return (S + 2) * u;
+}
+
+} // namespace eg::split

@@ -1,0 +1,342 @@
+// tcgen05 GEMM of the split-BF16 form (see split.cuh for the arithmetic).
+//
+// One persistent CTA per SM, 192 threads in three roles:
+//   warp 0      TMA producer: streams 128x64 BF16 tiles of the A and B digit
+//               planes (128-byte swizzle) into a 6-stage shared-memory ring;
+//   warp 1      MMA issuer: allocates 512 TMEM columns, issues
+//               tcgen05.mma kind::f16 (M=128, N=128, K=16) into one of two
+//               FP32 accumulators, and commits chunk completion;
+//   warps 2-5   epilogue: after every chunk of <= 1024 products per output,
+//               convert the exact FP32 sums to int64 and accumulate them in
+//               TMEM (columns 256..511 hold the low and high words), then at
+//               the end of a tile scale by 2^(eA+eB-...) in FP64 and apply
+//               C = cp*C + ab*v through the output's index map.
+// TMEM columns: [0,128) accumulator 0, [128,256) accumulator 1,
+//               [256,384) int64 low words, [384,512) int64 high words.
+// Every mbarrier wait is bounded (split.cuh, ptx.cuh): on a timeout the CTA
+// records an error code in *status, raises its abort flag, waits for its own
+// TMA loads and MMAs to land, frees TMEM and returns.
+#include <climits>
+
+#include "ptx.cuh"
+#include "split.cuh"
+
+namespace eg::split {
+
+namespace {
+
+constexpr int STAGES = 6;
+constexpr int A_BYTES = kBM * kBK * 2;
+constexpr int B_BYTES = kBN * kBK * 2;
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int THREADS = 192;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr int AUX_BYTES = 256;
+constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + AUX_BYTES + 4 * kBN * (8 + 4);
+constexpr int GROUP_M = 16; // tile rasterisation: groups of 16 row tiles share B tiles in L2
+constexpr unsigned long long DRAIN_NS = 200ull * 1000 * 1000;
+
+__device__ __forceinline__ void tile_coords(const TcGemmParams &p, int t, int &b, int &mt, int &nt) {
+    const int per_batch = p.mtiles * p.ntiles;
+    b = t / per_batch;
+    t -= b * per_batch;
+    const int per_group = GROUP_M * p.ntiles;
+    const int g = t / per_group;
+    const int first_m = g * GROUP_M;
+    const int gsize = min(p.mtiles - first_m, GROUP_M);
+    const int r = t - g * per_group;
+    mt = first_m + r % gsize;
+    nt = r / gsize;
+}
+
+__device__ __forceinline__ double scale_pow2(double v, int e) {
+    if (v == 0.0) return v;
+    const long long bits = __double_as_longlong(v);
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    const int ne = ex + e;
+    if (ex != 0 && ne > 0 && ne < 2047) return __longlong_as_double(bits + ((long long)e << 52));
+    return scalbn(v, e);
+}
+
+__device__ __forceinline__ void raise_abort(const TcGemmParams &p, volatile int *abort_flag, int code) {
+    atomicCAS(p.status, 0, code);
+    *abort_flag = 1;
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_tc_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                    const TcGemmParams p) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
+    uint64_t *empty = full + STAGES;
+    uint64_t *accf = empty + STAGES;
+    uint64_t *acce = accf + 2;
+    uint64_t *done = acce + 2;
+    uint32_t *tmem_slot = (uint32_t *)(done + 1);
+    volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+    // per-epilogue-warp copies of the tile's column offsets and exponents, so
+    // the epilogue warps never wait on one another
+    int64_t *colOffAll = (int64_t *)(smem + STAGES * STAGE_BYTES + AUX_BYTES);
+    int *colExpAll = (int *)(colOffAll + 4 * kBN);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < STAGES; i++) {
+            ptx::mbar_init(&full[i], 1);
+            ptx::mbar_init(&empty[i], 1);
+        }
+        for (int i = 0; i < 2; i++) {
+            ptx::mbar_init(&accf[i], 1);
+            ptx::mbar_init(&acce[i], 4);
+        }
+        ptx::mbar_init(done, 1);
+        *abort_flag = 0;
+        ptx::fence_mbar_init();
+    }
+    if (warp == 1) {
+        ptx::tmem_alloc(tmem_slot, TMEM_COLS);
+        ptx::tmem_relinquish();
+    }
+    ptx::tc_fence_before();
+    __syncthreads();
+    ptx::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int total_tiles = p.nbatch * p.mtiles * p.ntiles;
+    const int S = p.S;
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            ptx::tma_prefetch_desc(&tmA);
+            ptx::tma_prefetch_desc(&tmB);
+            int stage = 0;
+            uint32_t phase = 0;
+            bool issued[STAGES];
+            uint32_t issued_phase[STAGES];
+            for (int i = 0; i < STAGES; i++) {
+                issued[i] = false;
+                issued_phase[i] = 0;
+            }
+            bool ok = true;
+            for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
+                int b, mt, nt;
+                tile_coords(p, tile, b, mt, nt);
+                for (int d = 0; d < S && ok; d++) {
+                    const int kbs = (d + 1) * p.nkb;
+                    for (int j = 0; j < kbs; j++) {
+                        const int s = j / p.nkb, kb = j - s * p.nkb, t = d - s;
+                        if (!ptx::mbar_wait(&empty[stage], phase ^ 1, p.timeout_ns, abort_flag)) {
+                            raise_abort(p, abort_flag, 1);
+                            ok = false;
+                            break;
+                        }
+                        ptx::mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
+                        const int kc = (p.kb0 + kb) * kBK;
+                        uint8_t *sa = smem + stage * STAGE_BYTES;
+                        ptx::tma_load_3d(sa, &tmA, &full[stage], kc, mt * kBM, b * S + s);
+                        ptx::tma_load_3d(sa + A_BYTES, &tmB, &full[stage], kc, nt * kBN, b * S + t);
+                        issued[stage] = true;
+                        issued_phase[stage] = phase;
+                        if (++stage == STAGES) {
+                            stage = 0;
+                            phase ^= 1;
+                        }
+                    }
+                }
+            }
+            // Every load issued must land before the CTA may exit.
+            for (int i = 0; i < STAGES; i++)
+                if (issued[i] && !ptx::mbar_wait(&full[i], issued_phase[i], DRAIN_NS, nullptr))
+                    raise_abort(p, abort_flag, 4);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = ptx::idesc_bf16_f32(kBM, kBN);
+            int stage = 0;
+            uint32_t phase = 0;
+            int abuf = 0;
+            uint32_t aphase = 0;
+            bool ok = true;
+            for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
+                for (int d = 0; d < S && ok; d++) {
+                    const int kbs = (d + 1) * p.nkb;
+                    for (int c0 = 0; c0 < kbs && ok; c0 += kChunkKB) {
+                        const int c1 = min(c0 + kChunkKB, kbs);
+                        if (!ptx::mbar_wait(&acce[abuf], aphase ^ 1, p.timeout_ns, abort_flag)) {
+                            raise_abort(p, abort_flag, 2);
+                            ok = false;
+                            break;
+                        }
+                        ptx::tc_fence_after();
+                        const uint32_t dt = tmem + (uint32_t)(abuf * kBN);
+                        for (int j = c0; j < c1; j++) {
+                            if (!ptx::mbar_wait(&full[stage], phase, p.timeout_ns, abort_flag)) {
+                                raise_abort(p, abort_flag, 2);
+                                ok = false;
+                                break;
+                            }
+                            ptx::tc_fence_after();
+                            const uint32_t sa = ptx::smem_u32(smem + stage * STAGE_BYTES);
+                            const uint32_t sb = sa + A_BYTES;
+#pragma unroll
+                            for (int k = 0; k < kBK / 16; k++)
+                                ptx::mma_bf16(dt, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sb + k * 32),
+                                              idesc, (j > c0 || k > 0) ? 1u : 0u);
+                            ptx::mma_commit(&empty[stage]);
+                            if (++stage == STAGES) {
+                                stage = 0;
+                                phase ^= 1;
+                            }
+                        }
+                        if (!ok) break;
+                        ptx::mma_commit(&accf[abuf]);
+                        abuf ^= 1;
+                        if (abuf == 0) aphase ^= 1;
+                    }
+                }
+            }
+            // All issued MMAs must complete before TMEM is released.
+            ptx::mma_commit(done);
+            if (!ptx::mbar_wait(done, 0, DRAIN_NS, nullptr)) raise_abort(p, abort_flag, 5);
+        }
+    } else {
+        // ------------------------------------------------ epilogue (warps 2..5)
+        const int q = warp & 3;           // TMEM lane quadrant this warp may access
+        const int row = q * 32 + lane;    // tile row owned by this thread
+        const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16);
+        int64_t *colOff = colOffAll + (warp - 2) * kBN;
+        int *colExp = colExpAll + (warp - 2) * kBN;
+        int abuf = 0;
+        uint32_t aphase = 0;
+        bool ok = true;
+        for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
+            int b, mt, nt;
+            tile_coords(p, tile, b, mt, nt);
+            __syncwarp();
+            for (int i = lane; i < kBN; i += 32) {
+                const int64_t n = (int64_t)nt * kBN + i;
+                int64_t oa, ob, oc = 0;
+                int ex = 0;
+                if (n < p.N) {
+                    group_offsets32(p.ng, (uint32_t)n, oa, ob, oc);
+                    ex = p.eB[(int64_t)b * p.Np + n];
+                }
+                colOff[i] = oc;
+                colExp[i] = ex;
+            }
+            __syncwarp();
+            const int64_t m = (int64_t)mt * kBM + row;
+            const bool row_ok = m < p.M;
+            int64_t rowOff = 0, bOff = 0;
+            int rowExp = 0;
+            {
+                int64_t oa, ob;
+                if (row_ok) {
+                    group_offsets32(p.mg, (uint32_t)m, oa, ob, rowOff);
+                    rowExp = p.eA[(int64_t)b * p.Mp + m];
+                }
+                group_offsets(p.bg, b, oa, ob, bOff);
+            }
+            bool first = true;
+            for (int d = 0; d < S && ok; d++) {
+                const int kbs = (d + 1) * p.nkb;
+                for (int c0 = 0; c0 < kbs; c0 += kChunkKB) {
+                    bool w = ptx::mbar_wait(&accf[abuf], aphase, p.timeout_ns, abort_flag);
+                    w = __all_sync(0xffffffffu, w);
+                    if (!w) {
+                        if (lane == 0) raise_abort(p, abort_flag, 3);
+                        ok = false;
+                        break;
+                    }
+                    ptx::tc_fence_after();
+                    const bool shift = (c0 == 0) && !first;
+#pragma unroll 1
+                    for (int cc = 0; cc < kBN / 32; cc++) {
+                        uint32_t acc[32], lo[32], hi[32];
+                        ptx::tmem_ld32(tl + (uint32_t)(abuf * kBN + cc * 32), acc);
+                        if (!first) {
+                            ptx::tmem_ld32(tl + 256u + cc * 32, lo);
+                            ptx::tmem_ld32(tl + 384u + cc * 32, hi);
+                        }
+                        ptx::tmem_wait_ld();
+#pragma unroll
+                        for (int i = 0; i < 32; i++) {
+                            const long long x = (long long)__float2int_rn(__uint_as_float(acc[i]));
+                            long long R = first ? 0ll : (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
+                            if (shift) R *= 256;
+                            R += x;
+                            lo[i] = (uint32_t)((unsigned long long)R);
+                            hi[i] = (uint32_t)((unsigned long long)R >> 32);
+                        }
+                        ptx::tmem_st32(tl + 256u + cc * 32, lo);
+                        ptx::tmem_st32(tl + 384u + cc * 32, hi);
+                    }
+                    ptx::tmem_wait_st();
+                    ptx::tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) ptx::mbar_arrive(&acce[abuf]);
+                    abuf ^= 1;
+                    if (abuf == 0) aphase ^= 1;
+                    first = false;
+                }
+            }
+            if (!ok) break;
+            // final epilogue of the tile
+            const bool plain_store = p.zero && p.cp == 0.0;
+#pragma unroll 1
+            for (int cc = 0; cc < kBN / 32; cc++) {
+                uint32_t lo[32], hi[32];
+                ptx::tmem_ld32(tl + 256u + cc * 32, lo);
+                ptx::tmem_ld32(tl + 384u + cc * 32, hi);
+                ptx::tmem_wait_ld();
+                if (row_ok) {
+#pragma unroll 4
+                    for (int i = 0; i < 32; i++) {
+                        const int nl = cc * 32 + i;
+                        if ((int64_t)nt * kBN + nl >= p.N) break;
+                        const long long R = (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
+                        const int ce = colExp[nl];
+                        double v;
+                        if (rowExp == INT_MIN || ce == INT_MIN)
+                            v = __longlong_as_double(0x7ff8000000000000ll);
+                        else
+                            v = scale_pow2(__ll2double_rn(R), rowExp + ce + p.shift_const);
+                        double *cptr = p.C + bOff + rowOff + colOff[nl];
+                        *cptr = plain_store ? p.ab * v : fma(p.cp, *cptr, p.ab * v);
+                    }
+                }
+            }
+            ptx::tc_fence_before();
+        }
+    }
+
+    __syncthreads();
+    if (warp == 1) {
+        ptx::tc_fence_after();
+        ptx::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+} // namespace
+
+eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p, cudaStream_t s) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        EG_CUDA(cudaFuncSetAttribute(k_tc_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        attr_set = true;
+    }
+    const int total = p.nbatch * p.mtiles * p.ntiles;
+    if (total <= 0) return EG_SUCCESS;
+    const int grid = total < num_sms() ? total : num_sms();
+    {
+        LaunchScope ls_("k_tc_split_gemm", s);
+        k_tc_split_gemm<<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+    }
+    EG_CHECK_LAUNCH("k_tc_split_gemm");
+    return EG_SUCCESS;
+}
+
+} // namespace eg::split

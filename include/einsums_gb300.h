@@ -72,7 +72,7 @@ typedef struct eg_tensor {
 
 typedef struct eg_options {
     int32_t precision;    /* eg_precision */
-    int32_t slices;       /* split form: BF16 slices per operand, 2..8; 0 = chosen from `tolerance` */
+    int32_t slices;       /* split form: BF16 slices per operand, 2..6; 0 = chosen from `tolerance` */
     double tolerance;     /* split form: target relative Frobenius error (default 1e-10) */
     int32_t semantics;    /* eg_semantics */
     int32_t only_generic; /* report and run as the generic algorithm (OnlyUseGenericAlgorithm) */
@@ -149,6 +149,14 @@ eg_status eg_device_alloc(size_t bytes, void **ptr);
 eg_status eg_device_free(void *ptr);
 eg_status eg_set_memory_budget(size_t bytes);
 eg_status eg_memory_in_use(size_t *bytes);
+
+/* Error record of kernels with bounded device-side waits (the split form's tensor-core
+ * pipeline) for work issued on `stream`: synchronises the stream, returns EG_ERROR_TIMEOUT
+ * with the kernel's code in *device_code (may be NULL) when a wait gave up, and clears
+ * the record.  Such a kernel returns early instead of hanging, leaving its outputs
+ * incomplete; the context stays usable.  No reference counterpart (the reference's
+ * kernels have no bounded waits). */
+eg_status eg_stream_status(void *stream, int32_t *device_code);
 
 /* Host<->device copies on `stream` (DeviceTensor::read / operator= in DeviceTensor.hpp). */
 eg_status eg_copy_to_device(void *dst, const void *src, size_t bytes, void *stream);

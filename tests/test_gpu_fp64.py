@@ -28,7 +28,7 @@ def eg():
 
 
 def cu(x):
-    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+    return torch.from_numpy(np.array(x, dtype=np.float64, order="C", copy=True)).cuda()
 
 
 def cu_view(base_np, slicer):

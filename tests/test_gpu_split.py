@@ -1,0 +1,131 @@
+"""Parity of the split-BF16 tensor-core path with the CPU oracle (GPU).
+
+Tolerance: relative Frobenius error <= 1e-10 at the default 5 slices, and the
+error reported for every slice count (3..6) must fall with the count and stay
+under the a-priori bound the library reports."""
+import numpy as np
+import pytest
+
+import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL_SPLIT = 1e-10
+
+
+@pytest.fixture(scope="module")
+def eg():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import einsums_gb300
+    from einsums_gb300 import build
+    build.build()
+    return einsums_gb300
+
+
+def cu(x):
+    return torch.from_numpy(np.array(x, dtype=np.float64, order="C", copy=True)).cuda()
+
+
+def status_ok(eg):
+    import ctypes
+
+    from einsums_gb300 import _lib
+    code = ctypes.c_int32(0)
+    st = _lib.load().eg_stream_status(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream), ctypes.byref(code))
+    return st == 0 and code.value == 0
+
+
+def run_case(eg, Cl, Al, Bl, dims, cp=0.0, ab=1.0, slices=5, seed=0, scale_rows=False):
+    rng = np.random.default_rng(seed)
+    A = rng.standard_normal([dims[l] for l in Al])
+    B = rng.standard_normal([dims[l] for l in Bl])
+    if scale_rows:
+        A *= np.exp(rng.uniform(-30, 30, size=A.shape[:1]))[(...,) + (None,) * (A.ndim - 1)]
+    C = rng.standard_normal([dims[l] for l in Cl])
+    ref = C.copy()
+    oracle.einsum(Cl, ref, cp, ab, Al, A, Bl, B)
+    tC = cu(C)
+    eg.einsum(cp, Cl, tC, ab, Al, cu(A), Bl, cu(B), precision="split_bf16", slices=slices)
+    got = tC.cpu().numpy()
+    assert status_ok(eg)
+    return oracle.rel_fro(got, ref), eg.last_split_report()
+
+
+def test_single_tile_gemm(eg):
+    err, rep = run_case(eg, "ij", "ik", "kj", {"i": 128, "j": 128, "k": 64})
+    assert rep["slices"] == 5 and rep["slice_pairs"] == 15
+    assert err < TOL_SPLIT, err
+
+
+@pytest.mark.parametrize("dims", [{"i": 200, "j": 300, "k": 1000}, {"i": 37, "j": 129, "k": 70},
+                                  {"i": 1, "j": 250, "k": 3000}, {"i": 640, "j": 384, "k": 2500}])
+def test_gemm_shapes(eg, dims):
+    err, _ = run_case(eg, "ij", "ik", "kj", dims, cp=0.5, ab=-1.25)
+    assert err < TOL_SPLIT, err
+
+
+@pytest.mark.parametrize("S", [3, 4, 5, 6])
+def test_error_per_slice_count(eg, S):
+    err, rep = run_case(eg, "ikjl", "imjn", "mknl", {"i": 12, "k": 12, "j": 12, "l": 12, "m": 20, "n": 20}, slices=S,
+                        seed=S)
+    assert rep["slices"] == S and rep["slice_pairs"] == S * (S + 1) // 2
+    assert err <= 50 * rep["error_bound"], (S, err, rep)
+    if S >= 5:
+        assert err < TOL_SPLIT
+
+
+def test_generic_wmbej_pattern(eg):
+    err, _ = run_case(eg, "mbej", "jnfb", "mnef", {"m": 8, "b": 24, "e": 24, "j": 8, "n": 8, "f": 24}, cp=1.0,
+                      ab=-0.5)
+    assert err < TOL_SPLIT, err
+
+
+def test_wabef_pattern(eg):
+    err, _ = run_case(eg, "abef", "mnef", "mnab", {"a": 20, "b": 20, "e": 20, "f": 20, "m": 8, "n": 8}, cp=1.0,
+                      ab=0.25)
+    assert err < TOL_SPLIT, err
+
+
+def test_batched_pattern_and_gemv_shape(eg):
+    err, _ = run_case(eg, "bij", "bik", "bkj", {"b": 3, "i": 70, "j": 90, "k": 150})
+    assert err < TOL_SPLIT, err
+    err, _ = run_case(eg, "pq", "prqs", "rs", {"p": 12, "q": 12, "r": 12, "s": 12}, cp=1.0, ab=-1.0)
+    assert err < TOL_SPLIT, err
+
+
+def test_rows_with_wide_dynamic_range(eg):
+    err, _ = run_case(eg, "ij", "ik", "kj", {"i": 150, "j": 140, "k": 300}, scale_rows=True)
+    assert err < TOL_SPLIT, err
+
+
+def test_multi_pass_k_for_six_slices(eg):
+    # six slices sum at most 192 terms per pass, so K=700 takes four passes
+    err, _ = run_case(eg, "ij", "ik", "kj", {"i": 100, "j": 100, "k": 700}, cp=0.3, ab=2.0, slices=6)
+    assert err < 1e-12, err
+
+
+def test_nonfinite_row_gives_nan_row_only(eg):
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((64, 80))
+    B = rng.standard_normal((80, 48))
+    A[7, 3] = np.inf
+    tC = torch.zeros((64, 48), dtype=torch.float64, device="cuda")
+    eg.einsum(0.0, "ij", tC, 1.0, "ik", cu(A), "kj", cu(B), precision="split_bf16")
+    got = tC.cpu().numpy()
+    assert np.all(np.isnan(got[7]))
+    mask = np.ones(64, bool)
+    mask[7] = False
+    assert oracle.rel_fro(got[mask], (A @ B)[mask]) < TOL_SPLIT
+
+
+def test_deterministic(eg):
+    rng = np.random.default_rng(8)
+    A, B = cu(rng.standard_normal((300, 500))), cu(rng.standard_normal((500, 260)))
+    outs = []
+    for _ in range(2):
+        C = torch.zeros((300, 260), dtype=torch.float64, device="cuda")
+        eg.einsum(0.0, "ij", C, 1.0, "ik", A, "kj", B, precision="split_bf16")
+        outs.append(C.cpu().numpy())
+    assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))

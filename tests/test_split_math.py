@@ -1,0 +1,94 @@
+"""CPU check of the split-BF16 arithmetic used by the GPU kernels: row
+exponents, balanced base-256 digits (each exact in BF16), triangular
+truncation of the digit products, and exact integer accumulation.  A numpy
+restatement of einsums_gb300/csrc/split.cu:to_digits and the epilogue's
+R = sum_d 2^(8(S-1-d)) G_d; checks the reconstruction and the stated error
+bound, and the FP32-exactness limits the kernel relies on."""
+import math
+
+import numpy as np
+import pytest
+
+BITS, TOP = 8, 7
+
+
+def exponents(X):
+    mx = np.max(np.abs(X), axis=1)
+    e = np.zeros(len(mx), dtype=np.int64)
+    nz = mx > 0
+    _, e[nz] = np.frexp(mx[nz])
+    return e
+
+
+def digits(X, e, S):
+    """Balanced base-256 digits, leading digit first, like to_digits()."""
+    y = np.ldexp(X, (TOP + BITS * (S - 1) - e)[:, None])
+    F = np.rint(y).astype(np.int64)
+    out = np.zeros((S,) + X.shape, dtype=np.int64)
+    for s in range(S - 1, 0, -1):
+        d = F & 255
+        d = np.where(d > 128, d - 256, d)
+        out[s] = d
+        F = (F - d) // 256
+    out[0] = F
+    return out
+
+
+def split_product(A, B, S):
+    """A (M x K) times B^T (N x K) by the split scheme, with exact integers."""
+    eA, eB = exponents(A), exponents(B)
+    a, b = digits(A, eA, S), digits(B, eB, S)
+    R = np.zeros((A.shape[0], B.shape[0]), dtype=object)
+    for d in range(S):
+        G = sum(a[s].astype(object) @ b[d - s].T.astype(object) for s in range(d + 1))
+        R = R * 256 + G
+    shift = eA[:, None] + eB[None, :] - 2 * TOP - BITS * (S - 1)
+    out = np.empty(R.shape)
+    for i in range(R.shape[0]):
+        for j in range(R.shape[1]):
+            out[i, j] = math.ldexp(float(R[i, j]), int(shift[i, j]))
+    return out
+
+
+@pytest.mark.parametrize("S", [2, 3, 4, 5, 6])
+def test_digits_are_bf16_exact_and_reconstruct(S):
+    rng = np.random.default_rng(S)
+    X = rng.standard_normal((16, 40)) * np.exp(rng.uniform(-20, 20, size=(16, 1)))
+    X[3] = 0.0
+    e = exponents(X)
+    D = digits(X, e, S)
+    assert np.all(np.abs(D) <= 128)  # integers of magnitude <= 2^7: exact in BF16 (8 significant bits)
+    rec = sum(np.ldexp(D[s].astype(float), (e - TOP - BITS * s)[:, None]) for s in range(S))
+    # residual below half a unit of the last digit, relative to the row's 2^e
+    err = np.abs(rec - X) / np.ldexp(1.0, e)[:, None]
+    assert np.all(err <= 0.5 * 2.0 ** -(TOP + BITS * (S - 1)) + 1e-300)
+
+
+@pytest.mark.parametrize("S", [3, 4, 5, 6])
+def test_split_product_error_bound(S):
+    rng = np.random.default_rng(10 + S)
+    A = rng.standard_normal((12, 200))
+    B = rng.standard_normal((9, 200))
+    ref = A @ B.T
+    got = split_product(A, B, S)
+    scale = np.ldexp(1.0, exponents(A))[:, None] * np.ldexp(1.0, exponents(B))[None, :] * A.shape[1]
+    bound = (S + 2) * 2.0 ** -(TOP + BITS * (S - 1))
+    assert np.all(np.abs(got - ref) <= bound * scale)
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    if S >= 5:
+        assert rel < 1e-10
+
+
+def test_chunk_sums_stay_fp32_exact():
+    """1024 products of digits bounded by 128 stay within 2^24: the FP32
+    accumulators of one chunk hold exact integers."""
+    assert 1024 * 128 * 128 <= 2 ** 24
+
+
+def test_int64_accumulator_limit():
+    """R = sum_d 2^(8(S-1-d)) G_d stays below 2^62 for the per-pass K limit."""
+    for S in range(2, 7):
+        w = sum((d + 1) * 2.0 ** (8 * (S - 1 - d)) for d in range(S))
+        kmax = int(2 ** 62 / (2 ** 14 * w)) // 64 * 64
+        assert kmax * 2 ** 14 * w <= 2 ** 62
+        assert kmax >= 64
