@@ -313,6 +313,24 @@ eg_status einsum_impl(double cp, const int32_t *Cl, const eg_tensor *C, double a
     // (Dispatch.hpp:907, :343-346), so a NaN in C survives C_prefactor == 0 there.
     c.zero_when_cp_zero = !(opt.semantics == EG_SEMANTICS_CPP && (alg == Algorithm::DOT || alg == Algorithm::GER));
 
+    // A repeated C label addresses only C's diagonal; the prefactor still
+    // applies to all of C first (BaseAlgebra.hpp:129-133, PyTensorAlgebra.hpp:541-563).
+    bool c_repeats = false;
+    for (int i = 0; i < C->rank; i++)
+        for (int j = i + 1; j < C->rank; j++) c_repeats |= Cl[i] == Cl[j];
+    if (c_repeats && !(c.cp == 1.0)) {
+        ModeGroup cg;
+        for (int i = 0; i < C->rank; i++) {
+            cg.ext[cg.n] = C->extent[i];
+            cg.s[2][cg.n] = C->stride[i];
+            cg.total *= C->extent[i];
+            cg.n++;
+        }
+        if ((st = launch_scale(cg, C->data, c.cp, stream)) != EG_SUCCESS) return st;
+        c.cp = 1.0;
+        c.zero_when_cp_zero = false;
+    }
+
     const bool has_k = c.k.n > 0 || c.k.total == 0;
     if (opt.precision == EG_PRECISION_SPLIT_BF16 && c.k.total > 0 && (c.m.n > 0 || c.n.n > 0)) {
         eg_split_report rep{};

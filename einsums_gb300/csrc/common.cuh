@@ -124,6 +124,7 @@ class LaunchScope {
 
 // ------------------------------------------------------------- launchers --
 eg_status launch_elementwise(const Contraction &c, cudaStream_t s);
+eg_status launch_scale(const ModeGroup &g, double *C, double cp, cudaStream_t s);
 eg_status launch_dot(const Contraction &c, cudaStream_t s);
 eg_status launch_gemv(const Contraction &c, cudaStream_t s);
 eg_status launch_contract_f64(const Contraction &c, cudaStream_t s);

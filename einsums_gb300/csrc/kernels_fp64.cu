@@ -40,6 +40,23 @@ __global__ void k_elementwise(ModeGroup g, const double *__restrict__ A, const d
     }
 }
 
+// C = cp*C over every element of C (or C = 0 when cp == 0), walking C's own
+// modes; the prologue the reference applies to the whole output before a
+// generic contraction (BaseAlgebra.hpp:129-133), needed when C has repeated
+// labels and the contraction itself visits only its diagonal.
+template <bool Wide>
+__global__ void k_scale(ModeGroup g, double *C, double cp) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.total; i += stride) {
+        int64_t oa, ob, oc;
+        if (Wide)
+            group_offsets(g, i, oa, ob, oc);
+        else
+            group_offsets32(g, (uint32_t)i, oa, ob, oc);
+        C[oc] = cp == 0.0 ? 0.0 : cp * C[oc];
+    }
+}
+
 // ------------------------------------------------------ block reductions --
 template <int THREADS>
 __device__ __forceinline__ double block_sum(double v, double *smem) {
@@ -291,6 +308,20 @@ eg_status launch_elementwise(const Contraction &c, cudaStream_t s) {
         k_elementwise<true><<<grid, 256, 0, s>>>(g, c.A, c.B, c.C, c.cp, c.ab, c.zero_when_cp_zero);
         }
     EG_CHECK_LAUNCH("k_elementwise");
+    return EG_SUCCESS;
+}
+
+eg_status launch_scale(const ModeGroup &g, double *C, double cp, cudaStream_t s) {
+    if (g.total == 0) return EG_SUCCESS;
+    const int grid = grid_for(g.total, 256);
+    {
+        LaunchScope ls_("k_scale", s);
+        if (fits32(g))
+            k_scale<false><<<grid, 256, 0, s>>>(g, C, cp);
+        else
+            k_scale<true><<<grid, 256, 0, s>>>(g, C, cp);
+    }
+    EG_CHECK_LAUNCH("k_scale");
     return EG_SUCCESS;
 }
 
