@@ -64,7 +64,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -104,8 +104,9 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------- our arm --
-def ccd_step(eg, T, W, precision, slices, timers=None):
-    """The four contractions; returns nothing (results stay on the device)."""
+def ccd_step(eg, T, W, precision, slices, timers=None, report=None):
+    """The four contractions (results stay on the device).  When ``report`` is
+    a dict it receives the split-form accounting of the Wabef contraction."""
     import torch
     t, g = T["t"], T["g_oovv"]
 
@@ -124,6 +125,8 @@ def ccd_step(eg, T, W, precision, slices, timers=None):
                                    slices=slices))
     run("Wabef", lambda: eg.einsum(1.0, "abef", W["Wabef"], 0.25, "mnef", g, "mnab", t, precision=precision,
                                    slices=slices))
+    if report is not None:
+        report.update(eg.last_split_report())
     run("Wmbej", lambda: eg.einsum(1.0, "mbej", W["Wmbej"], -0.5, "jnfb", t, "mnef", g, precision=precision,
                                    slices=slices))
     run("E", lambda: eg.einsum(0.0, "", W["E"], 0.25, "ijab", t, "ijab", g))
@@ -240,8 +243,8 @@ def run_ours(args, rank, world):
     split_report = None
     if headline == "split_bf16":
         Ws = fresh_W(T)
-        ccd_step(eg, T, Ws, "split_bf16", args.slices)
-        split_report = core.last_split_report()
+        split_report = {}
+        ccd_step(eg, T, Ws, "split_bf16", args.slices, report=split_report)
         for k in ("Wmnij", "Wabef", "Wmbej"):
             errors[k] = rel_err(Ws[k] - T[{"Wmnij": "g_oooo", "Wabef": "g_vvvv", "Wmbej": "g_ovvo"}[k]],
                                 W64[k] - T[{"Wmnij": "g_oooo", "Wabef": "g_vvvv", "Wmbej": "g_ovvo"}[k]])

@@ -295,6 +295,13 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     p.eA = eA;
     p.eB = eB;
     p.shift_const = -2 * kTopBits - kBits * (S - 1);
+    {
+        int k = 0;
+        const double f = std::frexp(std::fabs(c.ab), &k); // |ab| = f 2^k
+        p.ab_pow2 = (f == 0.5) ? 1 : 0;
+        p.ab_neg = (p.ab_pow2 && c.ab < 0) ? 1 : 0;
+        if (p.ab_pow2) p.shift_const += k - 1;
+    }
     p.status = status;
     p.timeout_ns = 2000ull * 1000 * 1000;
 

@@ -41,10 +41,12 @@ struct TcGemmParams {
     ModeGroup bg, mg, ng; // output offsets in C (component 2)
     double *C;
     double cp, ab;
+    int ab_pow2; // ab = +-2^k: folded into the exponent (ab_neg gives the sign)
+    int ab_neg;
     int zero;
     const int *eA; // [nbatch][Mp] row exponents; INT_MIN marks a non-finite row
     const int *eB; // [nbatch][Np]
-    int shift_const; // -14 - 8 (S-1)
+    int shift_const; // -14 - 8 (S-1), plus k when ab = +-2^k
     int *status;
     unsigned long long timeout_ns;
 };

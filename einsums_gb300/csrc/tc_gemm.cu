@@ -1,12 +1,13 @@
 // tcgen05 GEMM of the split-BF16 form (see split.cuh for the arithmetic).
 //
-// One persistent CTA per SM, 192 threads in three roles:
+// One persistent CTA per SM, 320 threads in three roles:
 //   warp 0      TMA producer: streams 128x64 BF16 tiles of the A and B digit
 //               planes (128-byte swizzle) into a 6-stage shared-memory ring;
 //   warp 1      MMA issuer: allocates 512 TMEM columns, issues
 //               tcgen05.mma kind::f16 (M=128, N=128, K=16) into one of two
 //               FP32 accumulators, and commits chunk completion;
-//   warps 2-5   epilogue: after every chunk of <= 1024 products per output,
+//   warps 2-9   epilogue (two warps per TMEM lane quadrant, 64 columns each):
+//               after every chunk of <= 1024 products per output,
 //               convert the exact FP32 sums to int64 and accumulate them in
 //               TMEM (columns 256..511 hold the low and high words), then at
 //               the end of a tile scale by 2^(eA+eB-...) in FP64 and apply
@@ -29,10 +30,10 @@ constexpr int STAGES = 6;
 constexpr int A_BYTES = kBM * kBK * 2;
 constexpr int B_BYTES = kBN * kBK * 2;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int THREADS = 192;
+constexpr int THREADS = 320; // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int AUX_BYTES = 256;
-constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + AUX_BYTES + 4 * kBN * (8 + 4);
+constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + AUX_BYTES + 4 * kBN * (8 + 4);  // 8 warps x 64 columns
 constexpr int GROUP_M = 16; // tile rasterisation: groups of 16 row tiles share B tiles in L2
 constexpr unsigned long long DRAIN_NS = 200ull * 1000 * 1000;
 
@@ -63,7 +64,7 @@ __device__ __forceinline__ void raise_abort(const TcGemmParams &p, volatile int 
     *abort_flag = 1;
 }
 
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __maxnreg__(200)
     k_tc_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const TcGemmParams p) {
     extern __shared__ uint8_t smem_raw[];
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     // per-epilogue-warp copies of the tile's column offsets and exponents, so
     // the epilogue warps never wait on one another
     int64_t *colOffAll = (int64_t *)(smem + STAGES * STAGE_BYTES + AUX_BYTES);
-    int *colExpAll = (int *)(colOffAll + 4 * kBN);
+    int *colExpAll = (int *)(colOffAll + 4 * kBN); // 8 warps x 64 columns each
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         for (int i = 0; i < 2; i++) {
             ptx::mbar_init(&accf[i], 1);
-            ptx::mbar_init(&acce[i], 4);
+            ptx::mbar_init(&acce[i], 8);
         }
         ptx::mbar_init(done, 1);
         *abort_flag = 0;
@@ -203,23 +204,27 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (!ptx::mbar_wait(done, 0, DRAIN_NS, nullptr)) raise_abort(p, abort_flag, 5);
         }
     } else {
-        // ------------------------------------------------ epilogue (warps 2..5)
-        const int q = warp & 3;           // TMEM lane quadrant this warp may access
-        const int row = q * 32 + lane;    // tile row owned by this thread
+        // ------------------------------------------------ epilogue (warps 2..9)
+        // Two warps per TMEM lane quadrant; each owns 64 of the tile's 128 columns.
+        const int ew = warp - 2;              // 0..7
+        const int q = warp & 3;               // TMEM lane quadrant this warp may access
+        const int col0 = (ew >> 2) * (kBN / 2);
+        const int row = q * 32 + lane;        // tile row owned by this thread
         const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16);
-        int64_t *colOff = colOffAll + (warp - 2) * kBN;
-        int *colExp = colExpAll + (warp - 2) * kBN;
+        int64_t *colOff = colOffAll + ew * (kBN / 2);
+        int *colExp = colExpAll + ew * (kBN / 2);
         int abuf = 0;
         uint32_t aphase = 0;
         bool ok = true;
+        const bool plain_store = p.zero && p.cp == 0.0;
         for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
             int b, mt, nt;
             tile_coords(p, tile, b, mt, nt);
             __syncwarp();
-            for (int i = lane; i < kBN; i += 32) {
-                const int64_t n = (int64_t)nt * kBN + i;
+            for (int i = lane; i < kBN / 2; i += 32) {
+                const int64_t n = (int64_t)nt * kBN + col0 + i;
                 int64_t oa, ob, oc = 0;
-                int ex = 0;
+                int ex = INT_MAX; // marks a column beyond N
                 if (n < p.N) {
                     group_offsets32(p.ng, (uint32_t)n, oa, ob, oc);
                     ex = p.eB[(int64_t)b * p.Np + n];
@@ -254,12 +259,13 @@ __global__ void __launch_bounds__(THREADS, 1)
                     ptx::tc_fence_after();
                     const bool shift = (c0 == 0) && !first;
 #pragma unroll 1
-                    for (int cc = 0; cc < kBN / 32; cc++) {
+                    for (int cc = 0; cc < kBN / 64; cc++) {
+                        const uint32_t col = (uint32_t)(col0 + cc * 32);
                         uint32_t acc[32], lo[32], hi[32];
-                        ptx::tmem_ld32(tl + (uint32_t)(abuf * kBN + cc * 32), acc);
+                        ptx::tmem_ld32(tl + (uint32_t)(abuf * kBN) + col, acc);
                         if (!first) {
-                            ptx::tmem_ld32(tl + 256u + cc * 32, lo);
-                            ptx::tmem_ld32(tl + 384u + cc * 32, hi);
+                            ptx::tmem_ld32(tl + 256u + col, lo);
+                            ptx::tmem_ld32(tl + 384u + col, hi);
                         }
                         ptx::tmem_wait_ld();
 #pragma unroll
@@ -271,8 +277,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                             lo[i] = (uint32_t)((unsigned long long)R);
                             hi[i] = (uint32_t)((unsigned long long)R >> 32);
                         }
-                        ptx::tmem_st32(tl + 256u + cc * 32, lo);
-                        ptx::tmem_st32(tl + 384u + cc * 32, hi);
+                        ptx::tmem_st32(tl + 256u + col, lo);
+                        ptx::tmem_st32(tl + 384u + col, hi);
                     }
                     ptx::tmem_wait_st();
                     ptx::tc_fence_before();
@@ -284,28 +290,43 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
             }
             if (!ok) break;
-            // final epilogue of the tile
-            const bool plain_store = p.zero && p.cp == 0.0;
+            // final epilogue of the tile: C = cp*C + ab * R * 2^(eA+eB+shift)
+            const int64_t cbase = bOff + rowOff;
 #pragma unroll 1
-            for (int cc = 0; cc < kBN / 32; cc++) {
+            for (int cc = 0; cc < kBN / 64; cc++) {
+                const uint32_t col = (uint32_t)(col0 + cc * 32);
                 uint32_t lo[32], hi[32];
-                ptx::tmem_ld32(tl + 256u + cc * 32, lo);
-                ptx::tmem_ld32(tl + 384u + cc * 32, hi);
+                ptx::tmem_ld32(tl + 256u + col, lo);
+                ptx::tmem_ld32(tl + 384u + col, hi);
                 ptx::tmem_wait_ld();
                 if (row_ok) {
-#pragma unroll 4
-                    for (int i = 0; i < 32; i++) {
-                        const int nl = cc * 32 + i;
-                        if ((int64_t)nt * kBN + nl >= p.N) break;
-                        const long long R = (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
-                        const int ce = colExp[nl];
-                        double v;
-                        if (rowExp == INT_MIN || ce == INT_MIN)
-                            v = __longlong_as_double(0x7ff8000000000000ll);
-                        else
-                            v = scale_pow2(__ll2double_rn(R), rowExp + ce + p.shift_const);
-                        double *cptr = p.C + bOff + rowOff + colOff[nl];
-                        *cptr = plain_store ? p.ab * v : fma(p.cp, *cptr, p.ab * v);
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        // 16 loads first, so their latencies overlap
+                        double old[16];
+                        if (!plain_store) {
+#pragma unroll
+                            for (int i = 0; i < 16; i++) {
+                                const int c = cc * 32 + h * 16 + i;
+                                old[i] = colExp[c] != INT_MAX ? p.C[cbase + colOff[c]] : 0.0;
+                            }
+                        }
+#pragma unroll
+                        for (int i = 0; i < 16; i++) {
+                            const int c = cc * 32 + h * 16 + i;
+                            const int ce = colExp[c];
+                            if (ce == INT_MAX) continue;
+                            long long R = (long long)(((unsigned long long)hi[h * 16 + i] << 32) | lo[h * 16 + i]);
+                            if (p.ab_neg) R = -R;
+                            double v;
+                            if (rowExp == INT_MIN || ce == INT_MIN)
+                                v = __longlong_as_double(0x7ff8000000000000ll);
+                            else
+                                v = scale_pow2(__ll2double_rn(R), rowExp + ce + p.shift_const);
+                            if (!p.ab_pow2) v *= p.ab;
+                            double *cptr = p.C + cbase + colOff[c];
+                            *cptr = plain_store ? v : fma(p.cp, old[i], v);
+                        }
                     }
                 }
             }
