@@ -64,7 +64,9 @@ __device__ __forceinline__ void raise_abort(const TcGemmParams &p, volatile int 
     *abort_flag = 1;
 }
 
-__global__ void __maxnreg__(200)
+// 10 warps: two of the four SM sub-partitions hold three warps, so the
+// 16K-register file of a sub-partition caps a thread at 168 registers.
+__global__ void __launch_bounds__(THREADS, 1)
     k_tc_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const TcGemmParams p) {
     extern __shared__ uint8_t smem_raw[];
@@ -259,17 +261,17 @@ __global__ void __maxnreg__(200)
                     ptx::tc_fence_after();
                     const bool shift = (c0 == 0) && !first;
 #pragma unroll 1
-                    for (int cc = 0; cc < kBN / 64; cc++) {
-                        const uint32_t col = (uint32_t)(col0 + cc * 32);
-                        uint32_t acc[32], lo[32], hi[32];
-                        ptx::tmem_ld32(tl + (uint32_t)(abuf * kBN) + col, acc);
+                    for (int cc = 0; cc < kBN / 32; cc++) {
+                        const uint32_t col = (uint32_t)(col0 + cc * 16);
+                        uint32_t acc[16], lo[16], hi[16];
+                        ptx::tmem_ld16(tl + (uint32_t)(abuf * kBN) + col, acc);
                         if (!first) {
-                            ptx::tmem_ld32(tl + 256u + col, lo);
-                            ptx::tmem_ld32(tl + 384u + col, hi);
+                            ptx::tmem_ld16(tl + 256u + col, lo);
+                            ptx::tmem_ld16(tl + 384u + col, hi);
                         }
                         ptx::tmem_wait_ld();
 #pragma unroll
-                        for (int i = 0; i < 32; i++) {
+                        for (int i = 0; i < 16; i++) {
                             const long long x = (long long)__float2int_rn(__uint_as_float(acc[i]));
                             long long R = first ? 0ll : (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
                             if (shift) R *= 256;
@@ -277,8 +279,8 @@ __global__ void __maxnreg__(200)
                             lo[i] = (uint32_t)((unsigned long long)R);
                             hi[i] = (uint32_t)((unsigned long long)R >> 32);
                         }
-                        ptx::tmem_st32(tl + 256u + col, lo);
-                        ptx::tmem_st32(tl + 384u + col, hi);
+                        ptx::tmem_st16(tl + 256u + col, lo);
+                        ptx::tmem_st16(tl + 384u + col, hi);
                     }
                     ptx::tmem_wait_st();
                     ptx::tc_fence_before();
@@ -293,40 +295,37 @@ __global__ void __maxnreg__(200)
             // final epilogue of the tile: C = cp*C + ab * R * 2^(eA+eB+shift)
             const int64_t cbase = bOff + rowOff;
 #pragma unroll 1
-            for (int cc = 0; cc < kBN / 64; cc++) {
-                const uint32_t col = (uint32_t)(col0 + cc * 32);
-                uint32_t lo[32], hi[32];
-                ptx::tmem_ld32(tl + 256u + col, lo);
-                ptx::tmem_ld32(tl + 384u + col, hi);
+            for (int cc = 0; cc < kBN / 32; cc++) {
+                const uint32_t col = (uint32_t)(col0 + cc * 16);
+                uint32_t lo[16], hi[16];
+                ptx::tmem_ld16(tl + 256u + col, lo);
+                ptx::tmem_ld16(tl + 384u + col, hi);
                 ptx::tmem_wait_ld();
                 if (row_ok) {
-#pragma unroll
-                    for (int h = 0; h < 2; h++) {
-                        // 16 loads first, so their latencies overlap
-                        double old[16];
-                        if (!plain_store) {
-#pragma unroll
-                            for (int i = 0; i < 16; i++) {
-                                const int c = cc * 32 + h * 16 + i;
-                                old[i] = colExp[c] != INT_MAX ? p.C[cbase + colOff[c]] : 0.0;
-                            }
-                        }
+                    // 16 loads first, so their latencies overlap
+                    double old[16];
+                    if (!plain_store) {
 #pragma unroll
                         for (int i = 0; i < 16; i++) {
-                            const int c = cc * 32 + h * 16 + i;
-                            const int ce = colExp[c];
-                            if (ce == INT_MAX) continue;
-                            long long R = (long long)(((unsigned long long)hi[h * 16 + i] << 32) | lo[h * 16 + i]);
-                            if (p.ab_neg) R = -R;
-                            double v;
-                            if (rowExp == INT_MIN || ce == INT_MIN)
-                                v = __longlong_as_double(0x7ff8000000000000ll);
-                            else
-                                v = scale_pow2(__ll2double_rn(R), rowExp + ce + p.shift_const);
-                            if (!p.ab_pow2) v *= p.ab;
-                            double *cptr = p.C + cbase + colOff[c];
-                            *cptr = plain_store ? v : fma(p.cp, old[i], v);
+                            const int c = cc * 16 + i;
+                            old[i] = colExp[c] != INT_MAX ? p.C[cbase + colOff[c]] : 0.0;
                         }
+                    }
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        const int c = cc * 16 + i;
+                        const int ce = colExp[c];
+                        if (ce == INT_MAX) continue;
+                        long long R = (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
+                        if (p.ab_neg) R = -R;
+                        double v;
+                        if (rowExp == INT_MIN || ce == INT_MIN)
+                            v = __longlong_as_double(0x7ff8000000000000ll);
+                        else
+                            v = scale_pow2(__ll2double_rn(R), rowExp + ce + p.shift_const);
+                        if (!p.ab_pow2) v *= p.ab;
+                        double *cptr = p.C + cbase + colOff[c];
+                        *cptr = plain_store ? v : fma(p.cp, old[i], v);
                     }
                 }
             }
