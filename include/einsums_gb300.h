@@ -131,6 +131,20 @@ eg_status eg_einsum_batched(double C_prefactor, const int32_t *C_labels, const e
                             const eg_tensor *B_list, int64_t count, const eg_options *opt, void *stream,
                             int32_t *algorithm_choice);
 
+/*
+ * C = C_prefactor * C + AB_prefactor * sum_i A[i] * B[i] over n contiguous doubles, without
+ * allocating any device memory.  No counterpart in the reference: it is for callers that
+ * cannot let a library call cudaMalloc -- applications whose device memory is owned by
+ * another allocator (a framework's caching allocator or an arena reserved at start-up) and
+ * latency-critical loops that must not pay for an allocation.  The partial sums live in a
+ * fixed 32 KB array inside the library (4096 partials of 65536 elements each), so n is at
+ * most 2^28; longer inputs return EG_ERROR_NOT_SUPPORTED.  Every call on a device shares that
+ * array: calls whose kernels overlap on the GPU race.  The first call on a device, with that
+ * device current, looks the array up (cudaGetSymbolAddress); make it before any stream capture.
+ */
+eg_status eg_dot_noalloc(double C_prefactor, double *C, double AB_prefactor, const double *A, const double *B,
+                         int64_t n, void *stream);
+
 /* Split-form accounting for the last eg_einsum / eg_einsum_batched call on this host
  * thread: slices used per operand, BF16 slice-pair products issued, and the a-priori
  * relative error bound.  No reference counterpart (the reference has no split form). */
