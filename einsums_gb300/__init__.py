@@ -6,7 +6,7 @@ Importing it loads the CUDA library; there is no CPU fallback.
 """
 from . import _lib
 from .core import (ALGORITHMS, EinsumDirectProductPlan, EinsumDotPlan, EinsumGemmPlan, EinsumGemvPlan,
-                   EinsumGenericPlan, EinsumGerPlan, compile_plan, einsum, last_split_report, permute)
+                   EinsumGenericPlan, EinsumGerPlan, GroupedPlan, compile_plan, einsum, last_split_report, permute)
 
-__all__ = ["compile_plan", "einsum", "permute", "last_split_report", "ALGORITHMS", "EinsumGenericPlan",
+__all__ = ["compile_plan", "einsum", "permute", "GroupedPlan", "last_split_report", "ALGORITHMS", "EinsumGenericPlan",
            "EinsumDotPlan", "EinsumDirectProductPlan", "EinsumGerPlan", "EinsumGemvPlan", "EinsumGemmPlan"]

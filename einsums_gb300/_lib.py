@@ -81,6 +81,11 @@ PROTOTYPES = {
                                          ctypes.c_int64, _P(EgOptions), ctypes.c_void_p, _i32p]),
     "eg_dot_noalloc": (ctypes.c_int, [ctypes.c_double, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+    "eg_grouped_plan_create": (ctypes.c_int, [ctypes.c_double, _i32p, _T, ctypes.c_double, _i32p, _T, _i32p, _T,
+                                              ctypes.c_int64, _P(EgOptions), ctypes.c_void_p,
+                                              _P(ctypes.c_void_p), _i32p]),
+    "eg_grouped_plan_execute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "eg_grouped_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "eg_last_split_report": (ctypes.c_int, [_P(EgSplitReport)]),
     "eg_device_alloc": (ctypes.c_int, [ctypes.c_size_t, _P(ctypes.c_void_p)]),
     "eg_device_free": (ctypes.c_int, [ctypes.c_void_p]),

@@ -108,6 +108,50 @@ def _run_batched(C_prefactor, C_labels, Cs, AB_prefactor, A_labels, As, B_labels
     return alg.value
 
 
+class GroupedPlan:
+    """A list einsum lowered once and captured as a CUDA graph
+    (eg_grouped_plan_create); ``execute()`` replays it on the current stream.
+    The tensors must stay alive (and keep their storage) while the plan is used."""
+
+    def __init__(self, C_prefactor, C_indices, Cs, AB_prefactor, A_indices, As, B_indices, Bs, *,
+                 precision="fp64", slices=0, tolerance=1e-10, semantics=SEMANTICS_CPP, stream=None):
+        lib = _lib.load()
+        n = len(Cs)
+        if not (n == len(As) == len(Bs)) or n == 0:
+            raise ValueError("lists must be non-empty and of equal length")
+        self._keep = (list(Cs), list(As), list(Bs))
+        arrC, arrA, arrB = (EgTensor * n)(), (EgTensor * n)(), (EgTensor * n)()
+        for i in range(n):
+            if Cs[i].dim() != len(C_indices) or As[i].dim() != len(A_indices) or Bs[i].dim() != len(B_indices):
+                raise _lib.RankError(2, "tensor ranks do not match the indices")
+            _check_device(Cs[i], As[i], Bs[i])
+            arrC[i], arrA[i], arrB[i] = _tensor(Cs[i], "C"), _tensor(As[i], "A"), _tensor(Bs[i], "B")
+        opt = _options(precision, slices, semantics, False, tolerance)
+        handle = ctypes.c_void_p()
+        alg = ctypes.c_int32(-1)
+        _lib.check(lib.eg_grouped_plan_create(float(C_prefactor), _lib.labels(C_indices), arrC, float(AB_prefactor),
+                                              _lib.labels(A_indices), arrA, _lib.labels(B_indices), arrB, n,
+                                              ctypes.byref(opt), ctypes.c_void_p(_stream(stream)),
+                                              ctypes.byref(handle), ctypes.byref(alg)))
+        self._handle = handle
+        self.algorithm = ALGORITHMS[alg.value]
+        self.count = n
+
+    def execute(self, stream=None):
+        _lib.check(_lib.load().eg_grouped_plan_execute(self._handle, ctypes.c_void_p(_stream(stream))))
+
+    def close(self):
+        if getattr(self, "_handle", None):
+            _lib.load().eg_grouped_plan_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def classify(C_labels, A_labels, B_labels, semantics: int = SEMANTICS_CPP) -> int:
     lib = _lib.load()
     alg = ctypes.c_int32(-1)

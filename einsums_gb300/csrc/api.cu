@@ -345,6 +345,37 @@ eg_status einsum_impl(double cp, const int32_t *Cl, const eg_tensor *C, double a
     return launch_contract_f64(c, stream);
 }
 
+// Validates, classifies and lowers one item of a batch; gemm_shaped tells
+// whether it can join a grouped launch (summed modes, an output with more
+// than one position, no repeated output index).
+eg_status lower_for_group(double cp, const int32_t *Cl, const eg_tensor *C, double ab, const int32_t *Al,
+                          const eg_tensor *A, const int32_t *Bl, const eg_tensor *B, const eg_options &opt,
+                          Contraction &out, int32_t *alg_out, bool &gemm_shaped) {
+    eg_status st;
+    if ((st = check_tensor(C, Cl, "C")) != EG_SUCCESS) return st;
+    if ((st = check_tensor(A, Al, "A")) != EG_SUCCESS) return st;
+    if ((st = check_tensor(B, Bl, "B")) != EG_SUCCESS) return st;
+    Algorithm alg;
+    classify_labels(Cl, C->rank, Al, A->rank, Bl, B->rank, opt.semantics, alg);
+    if (opt.only_generic) alg = Algorithm::GENERIC;
+    if (opt.semantics == EG_SEMANTICS_CPP)
+        alg = detail::apply_vetoes(alg, labels_of(Cl, C->rank), view_of(C), labels_of(Al, A->rank), view_of(A),
+                                   labels_of(Bl, B->rank), view_of(B));
+    if (alg_out) *alg_out = (int32_t)alg;
+    Lowered low;
+    if ((st = lower(Cl, C, Al, A, Bl, B, opt.semantics, low)) != EG_SUCCESS) return st;
+    out = low.c;
+    out.cp = cp;
+    out.ab = ab;
+    out.zero_when_cp_zero = !(opt.semantics == EG_SEMANTICS_CPP && (alg == Algorithm::DOT || alg == Algorithm::GER));
+    bool c_repeats = false;
+    for (int i = 0; i < C->rank; i++)
+        for (int j = i + 1; j < C->rank; j++) c_repeats |= Cl[i] == Cl[j];
+    gemm_shaped = !low.empty_c && !c_repeats && out.k.n > 0 && out.k.total > 0 &&
+                  (out.m.n > 0 || out.n.n > 0 || out.batch.n > 0);
+    return EG_SUCCESS;
+}
+
 eg_status permute_impl(double cp, const int32_t *Cl, const eg_tensor *C, double ap, const int32_t *Al,
                        const eg_tensor *A, cudaStream_t stream) {
     eg_status st;

@@ -10,6 +10,7 @@
 namespace eg {
 namespace {
 std::atomic<uint64_t> g_launches{0};
+thread_local bool g_capture = false; // launches being captured into a graph are counted at replay
 std::atomic<int> g_enabled{0};
 struct Rec {
     const char *name;
@@ -49,7 +50,11 @@ eg_status drain() {
 }
 } // namespace
 
+void set_capture_mode(bool on) { g_capture = on; }
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 LaunchScope::LaunchScope(const char *name, cudaStream_t s) : name_(name), s_(s) {
+    if (g_capture) return;
     g_launches.fetch_add(1, std::memory_order_relaxed);
     if (g_enabled.load(std::memory_order_relaxed)) {
         std::lock_guard<std::mutex> lk(g_mu);

@@ -242,6 +242,10 @@ eg_status split_operand(const OperandMap &om, const double *X, unsigned long lon
 
 namespace eg {
 
+eg_status encode_planes_public(CUtensorMap *map, void *base, int64_t Kp, int64_t rows, int64_t planes) {
+    return split::encode_planes(map, base, Kp, rows, planes);
+}
+
 eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s, eg_split_report *rep) {
     using namespace split;
     const int S = slices ? slices : 5;

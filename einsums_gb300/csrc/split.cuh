@@ -51,7 +51,25 @@ struct TcGemmParams {
     unsigned long long timeout_ns;
 };
 
+// One item of a grouped launch: an independent contraction whose digit planes
+// start at plane zA / zB of the shared plane arrays and whose exponents start
+// at eAoff / eBoff.  Work entries (int4) are {item, batch index, mt, nt}.
+struct TcItem {
+    double *C;
+    int64_t M, N;
+    int nkb;
+    int zA, zB;
+    int eAoff, eBoff;
+    int Mp, Np;
+    ModeGroup bg, mg, ng;
+};
+
+// Sets the kernels' shared-memory attribute once (call outside stream capture).
+eg_status ensure_tc_attributes();
 eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p, cudaStream_t s);
+// Grouped form: `ntiles_total` work entries, per-tile parameters from `items`.
+eg_status launch_tc_gemm_grouped(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p,
+                                 const TcItem *items, const int4 *work, int ntiles_total, cudaStream_t s);
 
 // Largest K (a multiple of kBK) one pass may sum without the int64 accumulator
 // overflowing 2^62 for S slices.

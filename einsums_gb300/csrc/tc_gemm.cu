@@ -18,6 +18,7 @@
 // records an error code in *status, raises its abort flag, waits for its own
 // TMA loads and MMAs to land, frees TMEM and returns.
 #include <climits>
+#include <mutex>
 
 #include "ptx.cuh"
 #include "split.cuh"
@@ -50,6 +51,58 @@ __device__ __forceinline__ void tile_coords(const TcGemmParams &p, int t, int &b
     nt = r / gsize;
 }
 
+// Everything one role needs about a tile, for both the single-contraction and
+// the grouped form.
+struct TileJob {
+    int mt, nt;
+    int zA, zB;  // digit plane of slice 0 for A / B
+    int nkb;     // K blocks
+    int64_t M, N;
+    const ModeGroup *mg, *ng;
+    const int *eA, *eB; // exponents of rows / columns of this (item, batch)
+    double *C;          // output base of this (item, batch)
+};
+
+template <bool GROUPED>
+__device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *items, const int4 *work, int t) {
+    TileJob j;
+    if (!GROUPED) {
+        int b;
+        tile_coords(p, t, b, j.mt, j.nt);
+        j.zA = b * p.S;
+        j.zB = b * p.S;
+        j.nkb = p.nkb;
+        j.M = p.M;
+        j.N = p.N;
+        j.mg = &p.mg;
+        j.ng = &p.ng;
+        j.eA = p.eA + (int64_t)b * p.Mp;
+        j.eB = p.eB + (int64_t)b * p.Np;
+        int64_t oa, ob, oc;
+        group_offsets(p.bg, b, oa, ob, oc);
+        j.C = p.C + oc;
+    } else {
+        const int4 w = work[t];
+        const TcItem &it = items[w.x];
+        const int b = w.y;
+        j.mt = w.z;
+        j.nt = w.w;
+        j.zA = it.zA + b * p.S;
+        j.zB = it.zB + b * p.S;
+        j.nkb = it.nkb;
+        j.M = it.M;
+        j.N = it.N;
+        j.mg = &it.mg;
+        j.ng = &it.ng;
+        j.eA = p.eA + it.eAoff + (int64_t)b * it.Mp;
+        j.eB = p.eB + it.eBoff + (int64_t)b * it.Np;
+        int64_t oa, ob, oc;
+        group_offsets(it.bg, b, oa, ob, oc);
+        j.C = it.C + oc;
+    }
+    return j;
+}
+
 __device__ __forceinline__ double scale_pow2(double v, int e) {
     if (v == 0.0) return v;
     const long long bits = __double_as_longlong(v);
@@ -66,9 +119,10 @@ __device__ __forceinline__ void raise_abort(const TcGemmParams &p, volatile int 
 
 // 10 warps: two of the four SM sub-partitions hold three warps, so the
 // 16K-register file of a sub-partition caps a thread at 168 registers.
+template <bool GROUPED>
 __global__ void __launch_bounds__(THREADS, 1)
     k_tc_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                    const TcGemmParams p) {
+                    const __grid_constant__ TcGemmParams p, const TcItem *items, const int4 *work, int ntiles_total) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
@@ -106,7 +160,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     ptx::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    const int total_tiles = p.nbatch * p.mtiles * p.ntiles;
+    const int total_tiles = GROUPED ? ntiles_total : p.nbatch * p.mtiles * p.ntiles;
     const int S = p.S;
 
     if (warp == 0) {
@@ -124,12 +178,11 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             bool ok = true;
             for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
-                int b, mt, nt;
-                tile_coords(p, tile, b, mt, nt);
+                const TileJob job = resolve<GROUPED>(p, items, work, tile);
                 for (int d = 0; d < S && ok; d++) {
-                    const int kbs = (d + 1) * p.nkb;
+                    const int kbs = (d + 1) * job.nkb;
                     for (int j = 0; j < kbs; j++) {
-                        const int s = j / p.nkb, kb = j - s * p.nkb, t = d - s;
+                        const int s = j / job.nkb, kb = j - s * job.nkb, t = d - s;
                         if (!ptx::mbar_wait(&empty[stage], phase ^ 1, p.timeout_ns, abort_flag)) {
                             raise_abort(p, abort_flag, 1);
                             ok = false;
@@ -138,8 +191,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                         ptx::mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
                         const int kc = (p.kb0 + kb) * kBK;
                         uint8_t *sa = smem + stage * STAGE_BYTES;
-                        ptx::tma_load_3d(sa, &tmA, &full[stage], kc, mt * kBM, b * S + s);
-                        ptx::tma_load_3d(sa + A_BYTES, &tmB, &full[stage], kc, nt * kBN, b * S + t);
+                        ptx::tma_load_3d(sa, &tmA, &full[stage], kc, job.mt * kBM, job.zA + s);
+                        ptx::tma_load_3d(sa + A_BYTES, &tmB, &full[stage], kc, job.nt * kBN, job.zB + t);
                         issued[stage] = true;
                         issued_phase[stage] = phase;
                         if (++stage == STAGES) {
@@ -164,8 +217,9 @@ __global__ void __launch_bounds__(THREADS, 1)
             uint32_t aphase = 0;
             bool ok = true;
             for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
+                const int nkb = GROUPED ? items[work[tile].x].nkb : p.nkb;
                 for (int d = 0; d < S && ok; d++) {
-                    const int kbs = (d + 1) * p.nkb;
+                    const int kbs = (d + 1) * nkb;
                     for (int c0 = 0; c0 < kbs && ok; c0 += kChunkKB) {
                         const int c1 = min(c0 + kChunkKB, kbs);
                         if (!ptx::mbar_wait(&acce[abuf], aphase ^ 1, p.timeout_ns, abort_flag)) {
@@ -220,36 +274,32 @@ __global__ void __launch_bounds__(THREADS, 1)
         bool ok = true;
         const bool plain_store = p.zero && p.cp == 0.0;
         for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
-            int b, mt, nt;
-            tile_coords(p, tile, b, mt, nt);
+            const TileJob job = resolve<GROUPED>(p, items, work, tile);
             __syncwarp();
             for (int i = lane; i < kBN / 2; i += 32) {
-                const int64_t n = (int64_t)nt * kBN + col0 + i;
+                const int64_t n = (int64_t)job.nt * kBN + col0 + i;
                 int64_t oa, ob, oc = 0;
                 int ex = INT_MAX; // marks a column beyond N
-                if (n < p.N) {
-                    group_offsets32(p.ng, (uint32_t)n, oa, ob, oc);
-                    ex = p.eB[(int64_t)b * p.Np + n];
+                if (n < job.N) {
+                    group_offsets32(*job.ng, (uint32_t)n, oa, ob, oc);
+                    ex = job.eB[n];
                 }
                 colOff[i] = oc;
                 colExp[i] = ex;
             }
             __syncwarp();
-            const int64_t m = (int64_t)mt * kBM + row;
-            const bool row_ok = m < p.M;
-            int64_t rowOff = 0, bOff = 0;
+            const int64_t m = (int64_t)job.mt * kBM + row;
+            const bool row_ok = m < job.M;
+            int64_t rowOff = 0;
             int rowExp = 0;
-            {
+            if (row_ok) {
                 int64_t oa, ob;
-                if (row_ok) {
-                    group_offsets32(p.mg, (uint32_t)m, oa, ob, rowOff);
-                    rowExp = p.eA[(int64_t)b * p.Mp + m];
-                }
-                group_offsets(p.bg, b, oa, ob, bOff);
+                group_offsets32(*job.mg, (uint32_t)m, oa, ob, rowOff);
+                rowExp = job.eA[m];
             }
             bool first = true;
             for (int d = 0; d < S && ok; d++) {
-                const int kbs = (d + 1) * p.nkb;
+                const int kbs = (d + 1) * job.nkb;
                 for (int c0 = 0; c0 < kbs; c0 += kChunkKB) {
                     bool w = ptx::mbar_wait(&accf[abuf], aphase, p.timeout_ns, abort_flag);
                     w = __all_sync(0xffffffffu, w);
@@ -293,7 +343,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             if (!ok) break;
             // final epilogue of the tile: C = cp*C + ab * R * 2^(eA+eB+shift)
-            const int64_t cbase = bOff + rowOff;
+            double *const Cb = job.C;
+            const int64_t cbase = rowOff;
 #pragma unroll 1
             for (int cc = 0; cc < kBN / 32; cc++) {
                 const uint32_t col = (uint32_t)(col0 + cc * 16);
@@ -308,7 +359,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                         for (int i = 0; i < 16; i++) {
                             const int c = cc * 16 + i;
-                            old[i] = colExp[c] != INT_MAX ? p.C[cbase + colOff[c]] : 0.0;
+                            old[i] = colExp[c] != INT_MAX ? Cb[cbase + colOff[c]] : 0.0;
                         }
                     }
 #pragma unroll
@@ -324,7 +375,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         else
                             v = scale_pow2(__ll2double_rn(R), rowExp + ce + p.shift_const);
                         if (!p.ab_pow2) v *= p.ab;
-                        double *cptr = p.C + cbase + colOff[c];
+                        double *cptr = Cb + cbase + colOff[c];
                         *cptr = plain_store ? v : fma(p.cp, old[i], v);
                     }
                 }
@@ -342,20 +393,43 @@ __global__ void __launch_bounds__(THREADS, 1)
 
 } // namespace
 
+eg_status ensure_tc_attributes() {
+    static std::once_flag once;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [] {
+        err = cudaFuncSetAttribute(k_tc_split_gemm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_tc_split_gemm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    });
+    if (err != cudaSuccess) return cuda_fail(err, "cudaFuncSetAttribute(k_tc_split_gemm)");
+    return EG_SUCCESS;
+}
+
 eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p, cudaStream_t s) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        EG_CUDA(cudaFuncSetAttribute(k_tc_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        attr_set = true;
-    }
+    eg_status st = ensure_tc_attributes();
+    if (st != EG_SUCCESS) return st;
     const int total = p.nbatch * p.mtiles * p.ntiles;
     if (total <= 0) return EG_SUCCESS;
     const int grid = total < num_sms() ? total : num_sms();
     {
         LaunchScope ls_("k_tc_split_gemm", s);
-        k_tc_split_gemm<<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p);
+        k_tc_split_gemm<false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p, nullptr, nullptr, 0);
     }
     EG_CHECK_LAUNCH("k_tc_split_gemm");
+    return EG_SUCCESS;
+}
+
+eg_status launch_tc_gemm_grouped(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p,
+                                 const TcItem *items, const int4 *work, int ntiles_total, cudaStream_t s) {
+    eg_status st = ensure_tc_attributes();
+    if (st != EG_SUCCESS) return st;
+    if (ntiles_total <= 0) return EG_SUCCESS;
+    const int grid = ntiles_total < num_sms() ? ntiles_total : num_sms();
+    {
+        LaunchScope ls_("k_tc_split_gemm_grouped", s);
+        k_tc_split_gemm<true><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p, items, work, ntiles_total);
+    }
+    EG_CHECK_LAUNCH("k_tc_split_gemm_grouped");
     return EG_SUCCESS;
 }
 

@@ -120,8 +120,9 @@ eg_status eg_permute(double C_prefactor, const int32_t *C_labels, const eg_tenso
 
 /*
  * List einsum: item i computes C[i] = C_prefactor*C[i] + AB_prefactor * A[i]*B[i] with one
- * shared index pattern.  Items may have different extents.  Contractions that lower to a
- * matrix product run as one persistent grouped launch over a device-side work list.
+ * shared index pattern.  Items may have different extents.  Lists of contractions run as a
+ * grouped plan (see eg_grouped_plan_create), cached by call signature and replayed as a
+ * CUDA graph; other lists run item by item.
  * Replaces the batched overload einsum(C_prefactor, Cidx, &C_list, AB_prefactor, Aidx,
  * A_list, Bidx, B_list, &algorithm_choice) (Backends/Dispatch.hpp:1264-1286) and the list
  * form of Plan.execute (EinsumsPy/TensorAlgebra/src/Export.cpp:17-27).
@@ -144,6 +145,28 @@ eg_status eg_einsum_batched(double C_prefactor, const int32_t *C_labels, const e
  */
 eg_status eg_dot_noalloc(double C_prefactor, double *C, double AB_prefactor, const double *A, const double *B,
                          int64_t n, void *stream);
+
+/*
+ * Grouped plan: lowers every item of a list einsum once, builds a device-side work list of
+ * output tiles (largest first) and captures the batch as a CUDA graph -- one persistent
+ * grouped launch for FP64 (tile size per shape bucket from the autotuner's cache), or the
+ * digit-splitting launches plus one persistent tcgen05 launch for the split form.
+ * eg_grouped_plan_execute replays the graph on `stream`.  Items must be contractions over
+ * summed indices with a non-scalar, non-diagonal output; otherwise EG_ERROR_NOT_SUPPORTED
+ * (eg_einsum_batched then runs such lists item by item).  The plan keeps the tensors'
+ * addresses: they must stay valid while the plan is used.  Replaces the per-item OpenMP
+ * loop of the reference's list einsum (Backends/Dispatch.hpp:1264-1286) and the block loops
+ * of BlockAlgebra.hpp:23-50; *algorithm_choice receives item 0's algorithm.
+ */
+typedef struct eg_grouped_plan eg_grouped_plan;
+eg_status eg_grouped_plan_create(double C_prefactor, const int32_t *C_labels, const eg_tensor *C_list,
+                                 double AB_prefactor, const int32_t *A_labels, const eg_tensor *A_list,
+                                 const int32_t *B_labels, const eg_tensor *B_list, int64_t count,
+                                 const eg_options *opt, void *stream, eg_grouped_plan **plan,
+                                 int32_t *algorithm_choice);
+eg_status eg_grouped_plan_execute(eg_grouped_plan *plan, void *stream);
+/* Synchronises the plan's device and frees it. */
+eg_status eg_grouped_plan_destroy(eg_grouped_plan *plan);
 
 /* Split-form accounting for the last eg_einsum / eg_einsum_batched call on this host
  * thread: slices used per operand, BF16 slice-pair products issued, and the a-priori
