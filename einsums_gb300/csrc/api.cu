@@ -21,10 +21,13 @@ namespace {
 thread_local std::string g_last_error;
 thread_local eg_split_report g_split_report = {0, 0, 0, 0.0};
 
-std::mutex g_mem_mutex;
+// Library-wide registries are allocated once and never destroyed, so objects
+// released during static destruction at process exit (cached plans, workspaces)
+// never touch an already-destroyed container.
+std::mutex &g_mem_mutex = *new std::mutex;
 size_t g_budget = 0; // 0 = unlimited
 size_t g_in_use = 0;
-std::map<void *, size_t> g_sizes;
+std::map<void *, size_t> &g_sizes = *new std::map<void *, size_t>;
 
 struct WsKey {
     int dev;
@@ -35,8 +38,8 @@ struct WsBuf {
     void *ptr = nullptr;
     size_t bytes = 0;
 };
-std::mutex g_ws_mutex;
-std::map<WsKey, WsBuf> g_ws;
+std::mutex &g_ws_mutex = *new std::mutex;
+std::map<WsKey, WsBuf> &g_ws = *new std::map<WsKey, WsBuf>;
 } // namespace
 
 void set_error(const std::string &msg) { g_last_error = msg; }
@@ -108,8 +111,8 @@ eg_status workspace(cudaStream_t stream, size_t bytes, void **ptr) {
 void set_split_report(const eg_split_report &r) { g_split_report = r; }
 
 namespace {
-std::mutex g_status_mutex;
-std::map<WsKey, int *> g_status;
+std::mutex &g_status_mutex = *new std::mutex;
+std::map<WsKey, int *> &g_status = *new std::map<WsKey, int *>;
 } // namespace
 
 eg_status status_word(cudaStream_t stream, int **ptr) {

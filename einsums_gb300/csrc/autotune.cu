@@ -13,9 +13,9 @@
 namespace eg::autotune {
 
 namespace {
-std::mutex g_mu;
+std::mutex &g_mu = *new std::mutex;
 bool g_loaded = false;
-std::map<std::string, int> g_cache;
+std::map<std::string, int> &g_cache = *new std::map<std::string, int>;
 
 int ceil_log2(int64_t x) {
     int l = 0;

@@ -56,8 +56,10 @@ uint64_t fnv(uint64_t h, const void *p, size_t n) {
     return h;
 }
 
-std::mutex g_cache_mu;
-std::list<std::pair<uint64_t, std::shared_ptr<Plan>>> g_cache; // most recent first
+// Never destroyed: cached plans outlive static destruction at exit (their
+// device memory goes with the process).
+std::mutex &g_cache_mu = *new std::mutex;
+auto &g_cache = *new std::list<std::pair<uint64_t, std::shared_ptr<Plan>>>; // most recent first
 constexpr size_t kCacheSize = 8;
 
 struct StreamForCapture {

@@ -16,10 +16,10 @@ struct Rec {
     const char *name;
     cudaEvent_t e0, e1;
 };
-std::mutex g_mu;
-std::vector<Rec> g_pending;
-std::vector<cudaEvent_t> g_pool;
-std::map<std::string, std::pair<uint64_t, double>> g_totals;
+std::mutex &g_mu = *new std::mutex;
+std::vector<Rec> &g_pending = *new std::vector<Rec>;
+std::vector<cudaEvent_t> &g_pool = *new std::vector<cudaEvent_t>;
+auto &g_totals = *new std::map<std::string, std::pair<uint64_t, double>>;
 
 cudaEvent_t get_event() {
     if (!g_pool.empty()) {
