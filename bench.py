@@ -422,6 +422,228 @@ def run_reference(args, rank, world):
     }))
 
 
+# ------------------------------------------------------------ config suite --
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _time(fn, reps=3, warm=1):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = _events()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def suite_fock(eg, n=100):
+    """Config 1: F = 2 J - K with J = einsum(pq <- pqrs, rs) (GEMV) and K = einsum(pq <- prqs, rs) (GENERIC)."""
+    import numpy as np
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from einsums_gb300 import workloads
+    g_np, D_np = workloads.fock_inputs(n, seed=0)
+    g, D = torch.tensor(g_np, device="cuda"), torch.tensor(D_np, device="cuda")
+    F = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    out = {"config": f"Fock two-electron build n={n}"}
+    flop = 2.0 * n ** 4
+    for prec in ("fp64", "split_bf16"):
+        algJ = eg.einsum(0.0, "pq", F, 2.0, "pqrs", g, "rs", D, precision=prec)
+        msJ = _time(lambda: eg.einsum(0.0, "pq", F, 2.0, "pqrs", g, "rs", D, precision=prec))
+        msK = _time(lambda: eg.einsum(1.0, "pq", F, -1.0, "prqs", g, "rs", D, precision=prec))
+        F.zero_()
+        eg.einsum(0.0, "pq", F, 2.0, "pqrs", g, "rs", D, precision=prec)
+        algK = eg.einsum(1.0, "pq", F, -1.0, "prqs", g, "rs", D, precision=prec)
+        out[prec] = {"J_ms": msJ, "K_ms": msK, "J_alg": algJ, "K_alg": algK,
+                     "J_tflops": flop / msJ / 1e9, "K_tflops": flop / msK / 1e9,
+                     "J_gbs": 8.0 * n ** 4 / msJ / 1e6, "K_gbs": 8.0 * n ** 4 / msK / 1e6,
+                     "F": F.cpu().numpy().copy()}
+    Fref = np.zeros((n, n))
+    t0 = time.perf_counter()
+    oracle.einsum("pq", Fref, 0.0, 2.0, "pqrs", g_np, "rs", D_np)
+    tJ = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    oracle.einsum("pq", Fref, 1.0, -1.0, "prqs", g_np, "rs", D_np)
+    tK = time.perf_counter() - t0
+    for prec in ("fp64", "split_bf16"):
+        out[prec]["error_vs_oracle"] = oracle.rel_fro(out[prec].pop("F"), Fref)
+    out["cpu_oracle"] = {"J_ms": tJ * 1e3, "K_ms": tK * 1e3, "cores": host_cores()}
+    return out
+
+
+def suite_permute(eg, sizes=(32, 64, 128, 256)):
+    """Config 3a: all 24 rank-4 permutations at n^4, bit-exact."""
+    import itertools
+
+    import numpy as np
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    res = {"config": "rank-4 permute sweep, all 24 permutations", "sizes": {}}
+    pk, _ = peaks()
+    for n in sizes:
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(n)
+        A = torch.randn((n, n, n, n), generator=gen, dtype=torch.float64, device="cuda")
+        C = torch.empty_like(A)
+        back = torch.empty_like(A) if n >= 128 else None
+        times, exact = [], True
+        A_np = A.cpu().numpy() if n <= 64 else None
+        for perm in itertools.permutations(range(4)):
+            Cl = "".join("abcd"[p] for p in perm)
+            ms = _time(lambda: eg.permute(0.0, Cl, C, 1.0, "abcd", A), reps=3, warm=1)
+            times.append(ms)
+            if A_np is not None:
+                ref = np.empty([n] * 4)
+                oracle.permute(Cl, ref, 0.0, 1.0, "abcd", A_np)
+                exact &= bool(np.array_equal(C.cpu().numpy().view(np.uint64), ref.view(np.uint64)))
+            else:
+                # size-independent property: the inverse permutation restores A bit for bit
+                eg.permute(0.0, "abcd", back, 1.0, Cl, C)
+                exact &= bool(torch.equal(back.view(torch.int64), A.view(torch.int64)))
+        bytes_ = 16.0 * n ** 4
+        res["sizes"][str(n)] = {"mean_ms": sum(times) / len(times), "min_ms": min(times), "max_ms": max(times),
+                                "mean_gbs": bytes_ / (sum(times) / len(times)) / 1e6,
+                                "worst_gbs": bytes_ / max(times) / 1e6, "bit_exact": exact,
+                                "frac_of_hbm": bytes_ / (sum(times) / len(times)) / 1e6 / pk["hbm_gbs"]}
+        del A, C, back
+        torch.cuda.empty_cache()
+    return res
+
+
+def suite_contraction(eg, sizes=(64, 128)):
+    """Config 3b: C[i,k,j,l] = sum_mn A[i,m,j,n] B[m,k,n,l]; FP64 and split S = 3..6."""
+    import torch
+    from einsums_gb300 import workloads
+    res = {"config": "generic contraction ikjl <- imjn * mknl", "sizes": {}}
+    for n in sizes:
+        A, B = workloads.sweep_contraction_inputs(n, seed=n, backend="cuda")
+        C64 = torch.zeros((n, n, n, n), dtype=torch.float64, device="cuda")
+        flop = 2.0 * n ** 6
+        alg = eg.einsum(0.0, "ikjl", C64, 1.0, "imjn", A, "mknl", B)
+        ms64 = _time(lambda: eg.einsum(0.0, "ikjl", C64, 1.0, "imjn", A, "mknl", B), reps=1, warm=0)
+        entry = {"algorithm": alg, "fp64": {"ms": ms64, "tflops": flop / ms64 / 1e9}}
+        C = torch.zeros_like(C64)
+        for S in (3, 4, 5, 6):
+            ms = _time(lambda: eg.einsum(0.0, "ikjl", C, 1.0, "imjn", A, "mknl", B, precision="split_bf16",
+                                         slices=S), reps=2, warm=1)
+            err = float(torch.linalg.vector_norm(C - C64) / torch.linalg.vector_norm(C64))
+            entry[f"split_S{S}"] = {"ms": ms, "tflops": flop / ms / 1e9, "error_vs_fp64": err,
+                                    "speedup_vs_fp64": ms64 / ms}
+        res["sizes"][str(n)] = entry
+        del A, B, C, C64
+        torch.cuda.empty_cache()
+    return res
+
+
+def suite_batched(eg, count=2048):
+    """Config 4: 2048 contractions C_k[a,b] = sum_ij A_k[i,j,a] B_k[i,j,b], uneven extents."""
+    import numpy as np
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from einsums_gb300 import workloads
+    shapes = workloads.batched_shapes(count, seed=0)
+    As, Bs = workloads.batched_inputs(shapes, seed=1, backend="cuda")
+    Cs = [torch.zeros((a, b), dtype=torch.float64, device="cuda") for (i, j, a, b) in shapes]
+    flop = sum(2.0 * i * j * a * b for (i, j, a, b) in shapes)
+    res = {"config": f"{count} uneven contractions ab <- ija * ijb", "gflop": flop / 1e9}
+    sample = list(range(0, count, max(1, count // 16)))
+    for prec in ("fp64", "split_bf16"):
+        t0 = time.perf_counter()
+        plan = eg.GroupedPlan(0.0, "ab", Cs, 1.0, "ija", As, "ijb", Bs, precision=prec)
+        t_plan = time.perf_counter() - t0
+        ms_graph = _time(plan.execute, reps=5, warm=2)
+        errs = []
+        for k in sample:
+            ref = np.zeros(Cs[k].shape)
+            oracle.einsum("ab", ref, 0.0, 1.0, "ija", As[k].cpu().numpy(), "ijb", Bs[k].cpu().numpy())
+            errs.append(oracle.rel_fro(Cs[k].cpu().numpy(), ref))
+        plan.close()
+
+        def per_item():
+            for k in range(count):
+                eg.einsum(0.0, "ab", Cs[k], 1.0, "ija", As[k], "ijb", Bs[k], precision=prec)
+        ms_loop = _time(per_item, reps=1, warm=1)
+        res[prec] = {"grouped_graph_ms": ms_graph, "grouped_tflops": flop / ms_graph / 1e9,
+                     "plan_build_s": t_plan, "one_launch_per_contraction_ms": ms_loop,
+                     "speedup_vs_per_item": ms_loop / ms_graph, "max_error_vs_oracle_sample": max(errs)}
+    return res
+
+
+def suite_autograd(eg, o=24, v=96):
+    """Config 5: L = ||einsum(mbej <- jnfb, mnef)(t, g) - R||^2 with adjoint kernels."""
+    import numpy as np
+    import torch
+    from einsums_gb300 import autograd, workloads
+    T = workloads.ccd_inputs(o, v, seed=0, backend="cuda", with_vvvv=False)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(9)
+    R = torch.randn((o, v, v, o), generator=gen, dtype=torch.float64, device="cuda")
+    flop = 3 * 2.0 * o ** 3 * v ** 3
+    res = {"config": f"autograd Wmbej o={o} v={v}", "gflop_fwd_bwd": flop / 1e9}
+    grads = {}
+    for prec in ("fp64", "split_bf16"):
+        t = T["t"].clone().requires_grad_(True)
+        g = T["g_oovv"].clone().requires_grad_(True)
+
+        def step():
+            t.grad = None
+            g.grad = None
+            C = autograd.einsum_ag("mbej", "jnfb", "mnef", t, g, precision=prec)
+            ((C - R) ** 2).sum().backward()
+        ms = _time(step, reps=3, warm=1)
+        grads[prec] = (t.grad.clone(), g.grad.clone())
+        res[prec] = {"fwd_bwd_ms": ms, "tflops": flop / ms / 1e9}
+    for name, a, b in (("dt", grads["split_bf16"][0], grads["fp64"][0]), ("dg", grads["split_bf16"][1], grads["fp64"][1])):
+        res[f"split_error_{name}"] = float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+    # central differences (h = 1e-6) on 64 seeded entries of t and of g
+    rng = np.random.default_rng(4)
+    h = 1e-6
+    worst = 0.0
+    tt, gg = T["t"], T["g_oovv"]
+    for which, X in ((0, tt), (1, gg)):
+        grad = grads["fp64"][which]
+        gmax = float(grad.abs().max())
+        for f in rng.choice(X.numel(), size=64, replace=False):
+            idx = np.unravel_index(int(f), tuple(X.shape))
+            Xp, Xm = X.clone(), X.clone()
+            Xp[idx] += h
+            Xm[idx] -= h
+            args_p = (Xp, gg) if which == 0 else (tt, Xp)
+            args_m = (Xm, gg) if which == 0 else (tt, Xm)
+            Cp = autograd.einsum_ag("mbej", "jnfb", "mnef", *args_p).detach()
+            Cm = autograd.einsum_ag("mbej", "jnfb", "mnef", *args_m).detach()
+            fd = float(((Cp - Cm) * (Cp + Cm - 2.0 * R)).sum()) / (2 * h)
+            an = float(grad[idx])
+            worst = max(worst, abs(fd - an) / max(abs(an), 1e-3 * gmax))
+    res["fd_worst_relative_error"] = worst
+    return res
+
+
+def run_suite(args):
+    import torch
+
+    import einsums_gb300 as eg
+    torch.cuda.set_device(0)
+    which = args.suite.split(",") if args.suite != "all" else ["fock", "permute", "contraction", "batched", "autograd"]
+    fns = {"fock": suite_fock, "permute": suite_permute, "contraction": suite_contraction, "batched": suite_batched,
+           "autograd": suite_autograd}
+    for name in which:
+        t0 = time.perf_counter()
+        r = fns[name](eg)
+        r["suite"] = name
+        r["wall_s"] = time.perf_counter() - t0
+        print(json.dumps(r), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -433,7 +655,13 @@ def main():
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--suite", default=None,
+                    help="measure the other configurations instead (all, or a comma list of "
+                         "fock,permute,contraction,batched,autograd); one JSON line each")
     args = ap.parse_args()
+    if args.suite:
+        run_suite(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

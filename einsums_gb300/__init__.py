@@ -5,8 +5,9 @@ this package is its Python front end (``core``) plus the autograd binding.
 Importing it loads the CUDA library; there is no CPU fallback.
 """
 from . import _lib
+from .autograd import Einsum, einsum_ag
 from .core import (ALGORITHMS, EinsumDirectProductPlan, EinsumDotPlan, EinsumGemmPlan, EinsumGemvPlan,
                    EinsumGenericPlan, EinsumGerPlan, GroupedPlan, compile_plan, einsum, last_split_report, permute)
 
-__all__ = ["compile_plan", "einsum", "permute", "GroupedPlan", "last_split_report", "ALGORITHMS", "EinsumGenericPlan",
+__all__ = ["compile_plan", "einsum", "permute", "GroupedPlan", "Einsum", "einsum_ag", "last_split_report", "ALGORITHMS", "EinsumGenericPlan",
            "EinsumDotPlan", "EinsumDirectProductPlan", "EinsumGerPlan", "EinsumGemvPlan", "EinsumGemmPlan"]
