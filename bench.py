@@ -636,9 +636,10 @@ def run_suite(args):
     which = args.suite.split(",") if args.suite != "all" else ["fock", "permute", "contraction", "batched", "autograd"]
     fns = {"fock": suite_fock, "permute": suite_permute, "contraction": suite_contraction, "batched": suite_batched,
            "autograd": suite_autograd}
+    sizes = tuple(int(x) for x in args.sizes.split(",")) if args.sizes else None
     for name in which:
         t0 = time.perf_counter()
-        r = fns[name](eg)
+        r = fns[name](eg, sizes) if (sizes and name in ("permute", "contraction")) else fns[name](eg)
         r["suite"] = name
         r["wall_s"] = time.perf_counter() - t0
         print(json.dumps(r), flush=True)
@@ -658,6 +659,7 @@ def main():
     ap.add_argument("--suite", default=None,
                     help="measure the other configurations instead (all, or a comma list of "
                          "fock,permute,contraction,batched,autograd); one JSON line each")
+    ap.add_argument("--sizes", default=None, help="extents for the permute / contraction sweeps, e.g. 64,128")
     args = ap.parse_args()
     if args.suite:
         run_suite(args)
