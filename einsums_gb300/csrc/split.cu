@@ -12,6 +12,9 @@
 // the GEMM epilogue: nothing but the BF16 digit planes is materialised.
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -321,7 +324,30 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
         p.cp = first ? c.cp : 1.0;
         p.zero = first ? (c.zero_when_cp_zero ? 1 : 0) : 0;
         if (p.nkb <= 0) break;
+        static const bool prof_on = std::getenv("EINSUMS_GB300_TC_PROFILE") != nullptr;
+        unsigned long long *prof = nullptr;
+        if (prof_on) {
+            EG_CUDA(cudaMalloc(&prof, (size_t)num_sms() * 8 * sizeof(unsigned long long)));
+            EG_CUDA(cudaMemsetAsync(prof, 0, (size_t)num_sms() * 8 * sizeof(unsigned long long), s));
+        }
+        p.prof = prof;
         if ((st = launch_tc_gemm(tmA, tmB, p, s)) != EG_SUCCESS) return st;
+        if (prof) {
+            // Per-role wait/busy cycles summed over CTAs (a tracing aid, off by default).
+            std::vector<unsigned long long> h((size_t)num_sms() * 8);
+            EG_CUDA(cudaMemcpyAsync(h.data(), prof, h.size() * 8, cudaMemcpyDeviceToHost, s));
+            EG_CUDA(cudaStreamSynchronize(s));
+            cudaFree(prof);
+            double tot[8] = {0};
+            for (size_t i = 0; i < h.size(); i++) tot[i % 8] += (double)h[i];
+            std::fprintf(stderr,
+                         "[tc profile] M=%lld N=%lld K=%lld tiles=%d: total %.3g cyc/CTA | producer wait empty %.1f%% | "
+                         "mma wait full %.1f%% | mma wait acc %.1f%% | epi wait acc %.1f%% | epi flush %.1f%% | "
+                         "epi final %.1f%%\n",
+                         (long long)M, (long long)N, (long long)K, p.mtiles * p.ntiles * p.nbatch,
+                         tot[6] / num_sms(), 100 * tot[0] / tot[6], 100 * tot[1] / tot[6], 100 * tot[2] / tot[6],
+                         100 * tot[3] / tot[6], 100 * tot[4] / tot[6], 100 * tot[5] / tot[6]);
+        }
     }
     if (rep) {
         rep->slices = S;

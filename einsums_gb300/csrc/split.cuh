@@ -49,6 +49,8 @@ struct TcGemmParams {
     int shift_const; // -14 - 8 (S-1), plus k when ab = +-2^k
     int *status;
     unsigned long long timeout_ns;
+    // Optional per-CTA cycle counters (null in normal runs): see kProf* in tc_gemm.cu.
+    unsigned long long *prof;
 };
 
 // One item of a grouped launch: an independent contraction whose digit planes

@@ -38,6 +38,14 @@ constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + AUX_BYTES + 4 * kBN * (
 constexpr int GROUP_M = 16; // tile rasterisation: groups of 16 row tiles share B tiles in L2
 constexpr unsigned long long DRAIN_NS = 200ull * 1000 * 1000;
 
+// Optional cycle counters per CTA (TcGemmParams::prof, 8 slots per CTA).
+enum { kProfProducerWaitEmpty, kProfMmaWaitFull, kProfMmaWaitAcc, kProfEpiWaitAcc, kProfEpiFlush, kProfEpiFinal,
+       kProfTotal, kProfSlots = 8 };
+
+__device__ __forceinline__ void prof_add(const TcGemmParams &p, int slot, long long cycles) {
+    if (p.prof) atomicAdd(p.prof + blockIdx.x * kProfSlots + slot, (unsigned long long)cycles);
+}
+
 __device__ __forceinline__ void tile_coords(const TcGemmParams &p, int t, int &b, int &mt, int &nt) {
     const int per_batch = p.mtiles * p.ntiles;
     b = t / per_batch;
@@ -161,6 +169,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     int *colExpAll = (int *)(colOffAll + 4 * kBN); // 8 warps x 64 columns each
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long t_start = p.prof ? clock64() : 0;
     if (threadIdx.x == 0) {
         for (int i = 0; i < STAGES; i++) {
             ptx::mbar_init(&full[i], 1);
@@ -206,7 +215,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const int kbs = (d + 1) * job.nkb;
                     for (int j = 0; j < kbs; j++) {
                         const int s = j / job.nkb, kb = j - s * job.nkb, t = d - s;
-                        if (!ptx::mbar_wait(&empty[stage], phase ^ 1, p.timeout_ns, abort_flag)) {
+                        const long long t0 = p.prof ? clock64() : 0;
+                        const bool got = ptx::mbar_wait(&empty[stage], phase ^ 1, p.timeout_ns, abort_flag);
+                        if (p.prof) prof_add(p, kProfProducerWaitEmpty, clock64() - t0);
+                        if (!got) {
                             raise_abort(p, abort_flag, 1);
                             ok = false;
                             break;
@@ -245,7 +257,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const int kbs = (d + 1) * nkb;
                     for (int c0 = 0; c0 < kbs && ok; c0 += kChunkKB) {
                         const int c1 = min(c0 + kChunkKB, kbs);
-                        if (!ptx::mbar_wait(&acce[abuf], aphase ^ 1, p.timeout_ns, abort_flag)) {
+                        const long long ta = p.prof ? clock64() : 0;
+                        const bool got_acc = ptx::mbar_wait(&acce[abuf], aphase ^ 1, p.timeout_ns, abort_flag);
+                        if (p.prof) prof_add(p, kProfMmaWaitAcc, clock64() - ta);
+                        if (!got_acc) {
                             raise_abort(p, abort_flag, 2);
                             ok = false;
                             break;
@@ -253,7 +268,10 @@ __global__ void __launch_bounds__(THREADS, 1)
                         ptx::tc_fence_after();
                         const uint32_t dt = tmem + (uint32_t)(abuf * kBN);
                         for (int j = c0; j < c1; j++) {
-                            if (!ptx::mbar_wait(&full[stage], phase, p.timeout_ns, abort_flag)) {
+                            const long long tf = p.prof ? clock64() : 0;
+                            const bool got_full = ptx::mbar_wait(&full[stage], phase, p.timeout_ns, abort_flag);
+                            if (p.prof) prof_add(p, kProfMmaWaitFull, clock64() - tf);
+                            if (!got_full) {
                                 raise_abort(p, abort_flag, 2);
                                 ok = false;
                                 break;
@@ -324,7 +342,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int d = 0; d < S && ok; d++) {
                 const int kbs = (d + 1) * job.nkb;
                 for (int c0 = 0; c0 < kbs; c0 += kChunkKB) {
+                    const long long tw = (p.prof && ew == 0 && lane == 0) ? clock64() : 0;
                     bool w = ptx::mbar_wait(&accf[abuf], aphase, p.timeout_ns, abort_flag);
+                    const long long tw1 = (p.prof && ew == 0 && lane == 0) ? clock64() : 0;
+                    if (p.prof && ew == 0 && lane == 0) prof_add(p, kProfEpiWaitAcc, tw1 - tw);
                     w = __all_sync(0xffffffffu, w);
                     if (!w) {
                         if (lane == 0) raise_abort(p, abort_flag, 3);
@@ -359,6 +380,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     ptx::tc_fence_before();
                     __syncwarp();
                     if (lane == 0) ptx::mbar_arrive(&acce[abuf]);
+                    if (p.prof && ew == 0 && lane == 0) prof_add(p, kProfEpiFlush, clock64() - tw1);
                     abuf ^= 1;
                     if (abuf == 0) aphase ^= 1;
                     first = false;
@@ -366,6 +388,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
             if (!ok) break;
             // final epilogue of the tile: C = cp*C + ab * R * 2^(eA+eB+shift)
+            const long long tfin = (p.prof && ew == 0 && lane == 0) ? clock64() : 0;
             double *const Cb = job.C;
             const int64_t cbase = rowOff;
 #pragma unroll 1
@@ -404,10 +427,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
             }
             ptx::tc_fence_before();
+            if (p.prof && ew == 0 && lane == 0) prof_add(p, kProfEpiFinal, clock64() - tfin);
         }
     }
 
     __syncthreads();
+    if (p.prof && threadIdx.x == 0) prof_add(p, kProfTotal, clock64() - t_start);
     if (warp == 1) {
         ptx::tc_fence_after();
         ptx::tmem_dealloc(tmem, TMEM_COLS);
