@@ -633,8 +633,9 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
         dopsB[i].units_before = dprefB[i];
     }
 
-    void *planesA, *planesB, *maxA, *maxB, *eA, *eB, *d_opsA, *d_opsB, *d_dopsA, *d_dopsB, *d_items, *d_work;
+    void *planesA, *planesB, *maxA, *maxB, *eA, *eB, *d_opsA, *d_opsB, *d_dopsA, *d_dopsB, *d_items, *d_work, *rbuf;
     eg_status st;
+    if ((st = dev_alloc(plan, rbuf_bytes(), &rbuf)) != EG_SUCCESS) return st;
     if ((st = dev_alloc(plan, (size_t)zA * Rmax * Kmaxp * 2, &planesA)) != EG_SUCCESS) return st;
     if ((st = dev_alloc(plan, (size_t)zB * Rmax * Kmaxp * 2, &planesB)) != EG_SUCCESS) return st;
     if ((st = dev_alloc(plan, (size_t)rowsA * 8, &maxA)) != EG_SUCCESS) return st;
@@ -673,6 +674,7 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     }
     p.status = status;
     p.timeout_ns = 2000ull * 1000 * 1000;
+    p.rbuf = (long long *)rbuf;
 
     const int cap = num_sms() * 16;
     if ((st = ensure_tc_attributes()) != EG_SUCCESS) return st;

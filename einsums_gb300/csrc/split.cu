@@ -265,7 +265,8 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     const size_t offMaxB = offMaxA + round_up(nb * Mp * 8, 256);
     const size_t offEA = offMaxB + round_up(nb * Np * 8, 256);
     const size_t offEB = offEA + round_up(nb * Mp * 4, 256);
-    const size_t total = offEB + round_up(nb * Np * 4, 256);
+    const size_t offR = offEB + round_up(nb * Np * 4, 256);
+    const size_t total = offR + rbuf_bytes();
     void *ws = nullptr;
     eg_status st = workspace(s, total, &ws);
     if (st != EG_SUCCESS) return st;
@@ -311,6 +312,7 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     }
     p.status = status;
     p.timeout_ns = 2000ull * 1000 * 1000;
+    p.rbuf = (long long *)(base + offR);
 
     // K passes small enough for the exact int64 accumulator; later passes add into C.
     const int64_t kpass = max_k_per_pass(S);

@@ -51,6 +51,9 @@ struct TcGemmParams {
     unsigned long long timeout_ns;
     // Optional per-CTA cycle counters (null in normal runs): see kProf* in tc_gemm.cu.
     unsigned long long *prof;
+    // Per-CTA scratch of gridDim.x * 128 * 128 int64: a finished tile's sums
+    // wait here until the epilogue converts them during the next tile.
+    long long *rbuf;
 };
 
 // One item of a grouped launch: an independent contraction whose digit planes
@@ -72,6 +75,9 @@ eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const T
 // Grouped form: `ntiles_total` work entries, per-tile parameters from `items`.
 eg_status launch_tc_gemm_grouped(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p,
                                  const TcItem *items, const int4 *work, int ntiles_total, cudaStream_t s);
+
+// Bytes of the per-CTA sum scratch a tensor launch needs (TcGemmParams::rbuf).
+inline size_t rbuf_bytes() { return (size_t)num_sms() * kBM * kBN * sizeof(long long); }
 
 // Largest K (a multiple of kBK) one pass may sum without the int64 accumulator
 // overflowing 2^62 for S slices.

@@ -314,21 +314,49 @@ __global__ void __launch_bounds__(THREADS, 1)
         uint32_t aphase = 0;
         bool ok = true;
         const bool plain_store = p.zero && p.cp == 0.0;
+        // The previous ("pending") tile: its int64 sums wait in this CTA's scratch
+        // (this thread's row, 64 columns) and are finished 8 columns at a time
+        // after each flush of the next tile, so the FP64 epilogue never holds
+        // the accumulators the MMA issuer is waiting for.  colOff / colExp
+        // describe the pending tile.
+        long long *const rb = p.rbuf + ((size_t)blockIdx.x * kBM + row) * kBN + col0;
+        bool pend = false, pend_row_ok = false;
+        int pend_done = 0, pend_rowExp = 0;
+        double *pend_C = nullptr;
+        int64_t pend_rowOff = 0;
+        auto finalize_cols = [&](int upto) {
+            if (pend && pend_row_ok) {
+                for (int c0 = pend_done; c0 < upto; c0 += 8) {
+                    long long Rv[8];
+                    double old[8];
+#pragma unroll
+                    for (int i = 0; i < 8; i++) Rv[i] = rb[c0 + i];
+                    if (!plain_store) {
+#pragma unroll
+                        for (int i = 0; i < 8; i++)
+                            old[i] = colExp[c0 + i] != INT_MAX ? pend_C[pend_rowOff + colOff[c0 + i]] : 0.0;
+                    }
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        const int ce = colExp[c0 + i];
+                        if (ce == INT_MAX) continue;
+                        long long R = Rv[i];
+                        if (p.ab_neg) R = -R;
+                        double v;
+                        if (pend_rowExp == INT_MIN || ce == INT_MIN)
+                            v = __longlong_as_double(0x7ff8000000000000ll);
+                        else
+                            v = int64_times_pow2(R, pend_rowExp + ce + p.shift_const);
+                        if (!p.ab_pow2) v *= p.ab;
+                        double *cptr = pend_C + pend_rowOff + colOff[c0 + i];
+                        *cptr = plain_store ? v : (p.cp == 1.0 ? old[i] + v : fma(p.cp, old[i], v));
+                    }
+                }
+            }
+            pend_done = upto;
+        };
         for (int tile = blockIdx.x; tile < total_tiles && ok; tile += gridDim.x) {
             const TileJob job = resolve<GROUPED>(p, items, work, tile);
-            __syncwarp();
-            for (int i = lane; i < kBN / 2; i += 32) {
-                const int64_t n = (int64_t)job.nt * kBN + col0 + i;
-                int64_t oa, ob, oc = 0;
-                int ex = INT_MAX; // marks a column beyond N
-                if (n < job.N) {
-                    group_offsets32(*job.ng, (uint32_t)n, oa, ob, oc);
-                    ex = job.eB[n];
-                }
-                colOff[i] = oc;
-                colExp[i] = ex;
-            }
-            __syncwarp();
             const int64_t m = (int64_t)job.mt * kBM + row;
             const bool row_ok = m < job.M;
             int64_t rowOff = 0;
@@ -384,13 +412,16 @@ __global__ void __launch_bounds__(THREADS, 1)
                     abuf ^= 1;
                     if (abuf == 0) aphase ^= 1;
                     first = false;
+                    // a slice of the pending tile while the MMAs run
+                    if (pend_done < kBN / 2) finalize_cols(pend_done + 8);
                 }
             }
             if (!ok) break;
-            // final epilogue of the tile: C = cp*C + ab * R * 2^(eA+eB+shift)
+            // end of tile: finish the pending tile, park this tile's sums in the
+            // scratch, and make this tile the pending one
             const long long tfin = (p.prof && ew == 0 && lane == 0) ? clock64() : 0;
-            double *const Cb = job.C;
-            const int64_t cbase = rowOff;
+            finalize_cols(kBN / 2);
+            __syncwarp();
 #pragma unroll 1
             for (int cc = 0; cc < kBN / 32; cc++) {
                 const uint32_t col = (uint32_t)(col0 + cc * 16);
@@ -398,37 +429,32 @@ __global__ void __launch_bounds__(THREADS, 1)
                 ptx::tmem_ld16(tl + 256u + col, lo);
                 ptx::tmem_ld16(tl + 384u + col, hi);
                 ptx::tmem_wait_ld();
-                if (row_ok) {
-                    // 16 loads first, so their latencies overlap
-                    double old[16];
-                    if (!plain_store) {
 #pragma unroll
-                        for (int i = 0; i < 16; i++) {
-                            const int c = cc * 16 + i;
-                            old[i] = colExp[c] != INT_MAX ? Cb[cbase + colOff[c]] : 0.0;
-                        }
-                    }
-#pragma unroll
-                    for (int i = 0; i < 16; i++) {
-                        const int c = cc * 16 + i;
-                        const int ce = colExp[c];
-                        if (ce == INT_MAX) continue;
-                        long long R = (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
-                        if (p.ab_neg) R = -R;
-                        double v;
-                        if (rowExp == INT_MIN || ce == INT_MIN)
-                            v = __longlong_as_double(0x7ff8000000000000ll);
-                        else
-                            v = int64_times_pow2(R, rowExp + ce + p.shift_const);
-                        if (!p.ab_pow2) v *= p.ab;
-                        double *cptr = Cb + cbase + colOff[c];
-                        *cptr = plain_store ? v : (p.cp == 1.0 ? old[i] + v : fma(p.cp, old[i], v));
-                    }
-                }
+                for (int i = 0; i < 16; i++)
+                    rb[cc * 16 + i] = (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
             }
             ptx::tc_fence_before();
+            for (int i = lane; i < kBN / 2; i += 32) {
+                const int64_t n = (int64_t)job.nt * kBN + col0 + i;
+                int64_t oa, ob, oc = 0;
+                int ex = INT_MAX; // marks a column beyond N
+                if (n < job.N) {
+                    group_offsets32(*job.ng, (uint32_t)n, oa, ob, oc);
+                    ex = job.eB[n];
+                }
+                colOff[i] = oc;
+                colExp[i] = ex;
+            }
+            __syncwarp();
+            pend = true;
+            pend_done = 0;
+            pend_row_ok = row_ok;
+            pend_rowExp = rowExp;
+            pend_rowOff = rowOff;
+            pend_C = job.C;
             if (p.prof && ew == 0 && lane == 0) prof_add(p, kProfEpiFinal, clock64() - tfin);
         }
+        if (ok) finalize_cols(kBN / 2);
     }
 
     __syncthreads();
