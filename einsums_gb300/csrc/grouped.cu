@@ -547,13 +547,14 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     const int S = slices ? slices : 5;
     if (S < 2 || S > kMaxSlices) return fail(EG_ERROR_INVALID_ARGUMENT, "split form: slices must be in 2..6");
     const int64_t kmax = max_k_per_pass(S);
-    int64_t Rmax = kBM, Kmaxp = kBK, zA = 0, zB = 0, rowsA = 0, rowsB = 0;
+    int64_t Rmax = kBM, Kmaxp = kKStep, zA = 0, zB = 0, rowsA = 0, rowsB = 0;
     for (auto &c : cs) {
         if (c.k.total > kmax) return fail(EG_ERROR_NOT_SUPPORTED, "grouped split: K above one exact pass");
+        if (c.k.total <= 0) return fail(EG_ERROR_NOT_SUPPORTED, "grouped split: an item sums over no index");
         if (c.m.total >= (1ll << 31) || c.n.total >= (1ll << 31) || c.k.total >= (1ll << 31))
             return fail(EG_ERROR_NOT_SUPPORTED, "grouped split: extent above 2^31");
         Rmax = std::max({Rmax, round_up(c.m.total, kBM), round_up(c.n.total, kBN)});
-        Kmaxp = std::max(Kmaxp, round_up(c.k.total, kBK));
+        Kmaxp = std::max(Kmaxp, round_up(c.k.total, kKStep));
     }
     std::vector<GOp> opsA, opsB;
     std::vector<TcItem> items;
@@ -563,7 +564,7 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     for (size_t i = 0; i < cs.size(); i++) {
         const Contraction &c = cs[i];
         const int64_t nb = c.batch.total, M = c.m.total, N = c.n.total, K = c.k.total;
-        const int64_t Kp = round_up(K, kBK), Mp = round_up(M, kBM), Np = round_up(N, kBN);
+        const int64_t Kp = round_up(K, kKStep), Mp = round_up(M, kBM), Np = round_up(N, kBN);
         GOp a{};
         a.X = c.A;
         a.bg = c.batch;

@@ -258,7 +258,7 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     if (M >= (int64_t(1) << 31) || N >= (int64_t(1) << 31) || K >= (int64_t(1) << 31) || nb * S >= (int64_t(1) << 31))
         return fail(EG_ERROR_NOT_SUPPORTED, "split form: a mode group exceeds 2^31 elements");
     // rows of A padded to whole pairs of tiles, so cluster pairs never run past the planes
-    const int64_t Kp = round_up(K, kBK), Mp = round_up(M, 2 * kBM), Np = round_up(N, kBN);
+    const int64_t Kp = round_up(K, kKStep), Mp = round_up(M, 2 * kBM), Np = round_up(N, kBN);
 
     // workspace: digit planes of A and B, row maxima, exponents, status word
     const size_t bytesA = (size_t)nb * S * Mp * Kp * 2, bytesB = (size_t)nb * S * Np * Kp * 2;
@@ -344,13 +344,15 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
             EG_CUDA(cudaStreamSynchronize(s));
             cudaFree(prof);
             double tot[8] = {0};
+            int ran = 0; // CTAs of the launch (its grid may be below the SM count)
             for (size_t i = 0; i < h.size(); i++) tot[i % 8] += (double)h[i];
+            for (size_t i = 6; i < h.size(); i += 8) ran += h[i] > 0 ? 1 : 0;
             std::fprintf(stderr,
                          "[tc profile] M=%lld N=%lld K=%lld tiles=%d: total %.3g cyc/CTA | producer wait empty %.1f%% | "
                          "mma wait full %.1f%% | mma wait acc %.1f%% | epi wait acc %.1f%% | epi flush %.1f%% | "
                          "epi final %.1f%%\n",
                          (long long)M, (long long)N, (long long)K, p.mtiles * p.ntiles * p.nbatch,
-                         tot[6] / num_sms(), 100 * tot[0] / tot[6], 100 * tot[1] / tot[6], 100 * tot[2] / tot[6],
+                         tot[6] / (ran > 0 ? ran : 1), 100 * tot[0] / tot[6], 100 * tot[1] / tot[6], 100 * tot[2] / tot[6],
                          100 * tot[3] / tot[6], 100 * tot[4] / tot[6], 100 * tot[5] / tot[6]);
         }
     }

@@ -30,6 +30,7 @@ constexpr int kTopBits = 7;     // magnitude bits of the leading digit
 constexpr int kMaxSlices = 6;   // keeps the scaled digits and the int64 accumulator in range
 constexpr int kBM = 128, kBN = 128, kBK = 64;
 constexpr int kChunkKB = 16;    // 16 x 64 = 1024 products per exact FP32 chunk
+constexpr int kKStep = 2 * kBK;  // K is padded to whole groups of two K blocks
 
 struct TcGemmParams {
     int S;
@@ -82,15 +83,15 @@ eg_status launch_tc_gemm_grouped(const CUtensorMap &tmA, const CUtensorMap &tmB,
 // Bytes of the per-CTA sum scratch a tensor launch needs (TcGemmParams::rbuf).
 inline size_t rbuf_bytes() { return (size_t)num_sms() * kBM * kBN * sizeof(long long); }
 
-// Largest K (a multiple of kBK) one pass may sum without the int64 accumulator
-// overflowing 2^62 for S slices.
+// Largest K (a multiple of kKStep) one pass may sum without the int64
+// accumulator overflowing 2^62 for S slices.
 inline int64_t max_k_per_pass(int S) {
     // |R| <= K * 2^14 * sum_d (d+1) 2^(8 (S-1-d))
     double w = 0.0;
     for (int d = 0; d < S; d++) w += (d + 1) * std::ldexp(1.0, 8 * (S - 1 - d));
     double kmax = std::ldexp(1.0, 62) / (std::ldexp(1.0, 14) * w);
     int64_t k = (int64_t)kmax;
-    return (k / kBK) * kBK;
+    return (k / kKStep) * kKStep;
 }
 
 // A-priori bound on the relative error of one product, relative to

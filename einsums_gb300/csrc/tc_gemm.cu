@@ -2,10 +2,17 @@
 //
 // One persistent CTA per SM, 320 threads in three roles:
 //   warp 0      TMA producer: streams 128x64 BF16 tiles of the A and B digit
-//               planes (128-byte swizzle) into a 6-stage shared-memory ring;
+//               planes (128-byte swizzle) into a 3-slot shared-memory ring;
+//               a slot holds up to two consecutive 64-wide K blocks of one
+//               slice pair (a "group", 64 KB);
 //   warp 1      MMA issuer: allocates 512 TMEM columns, issues
-//               tcgen05.mma kind::f16 (M=128, N=128, K=16) into one of two
-//               FP32 accumulators, and commits chunk completion;
+//               tcgen05.mma kind::f16 (M=128, N=128, K=16), eight per group,
+//               into one of two FP32 accumulators, and commits chunk
+//               completion.  A blocking mbarrier wait costs the issuing
+//               thread ~140 cycles, longer than the two MMAs the tensor pipe
+//               keeps queued, so the issuer tests the next slot's barrier
+//               without blocking in the same instruction sequence as the
+//               current group's MMAs and waits only when that test failed;
 //   warps 2-9   epilogue (two warps per TMEM lane quadrant, 64 columns each):
 //               after every chunk of <= 1024 products per output,
 //               convert the exact FP32 sums to int64 and accumulate them in
@@ -19,6 +26,7 @@
 // TMA loads and MMAs to land, frees TMEM and returns.
 #include <climits>
 #include <mutex>
+#include <type_traits>
 
 #include "ptx.cuh"
 #include "split.cuh"
@@ -27,10 +35,12 @@ namespace eg::split {
 
 namespace {
 
-constexpr int STAGES = 6;
-constexpr int A_BYTES = kBM * kBK * 2;
-constexpr int B_BYTES = kBN * kBK * 2;
-constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int STAGES = 3;                  // ring slots
+constexpr int GROUP_KB = 2;                // K blocks per slot
+constexpr int A_BYTES = kBM * kBK * 2;     // one K block of A (16 KB)
+constexpr int B_BYTES = kBN * kBK * 2;     // one K block of B (16 KB)
+constexpr int KB_BYTES = A_BYTES + B_BYTES;
+constexpr int STAGE_BYTES = GROUP_KB * KB_BYTES;  // [A kb0][A kb1][B kb0][B kb1]
 constexpr int THREADS = 320; // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int AUX_BYTES = 256;
@@ -155,6 +165,58 @@ __device__ __forceinline__ double int64_times_pow2(long long R, int e) {
     return __longlong_as_double((long long)(sign | ((unsigned long long)biased << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
+// Issues the 4 * NB MMAs of one group (K blocks at A/B descriptors a0, b0;
+// a second block sits A_BYTES / B_BYTES further on) and, in the same
+// instruction sequence, tests whether phase `parity` of the barrier at
+// `next_bar` has completed.  The test's result is read after the MMAs are
+// issued, so its latency overlaps their execution.
+template <int NB>
+__device__ __forceinline__ bool mma_group(uint32_t d, uint64_t a0, uint64_t b0, uint32_t idesc, uint32_t accumulate,
+                                          uint32_t next_bar, uint32_t parity) {
+    static_assert(NB == 1 || NB == 2, "one or two K blocks per group");
+    constexpr uint64_t kStep = 32 >> 4;            // 16 BF16 along K
+    constexpr uint64_t aBlk = A_BYTES >> 4, bBlk = B_BYTES >> 4;
+    uint32_t ok;
+    if (NB == 1) {
+        asm volatile(
+            "{\n .reg .pred p, q;\n setp.ne.b32 q, %4, 0;\n"
+            " mbarrier.test_wait.parity.shared::cta.b64 p, [%5], %6;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], %2, %3, %7, q;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], %8, %9, %7, 1;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], %10, %11, %7, 1;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], %12, %13, %7, 1;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(d), "l"(a0), "l"(b0), "r"(accumulate), "r"(next_bar), "r"(parity), "r"(idesc),
+              "l"(a0 + kStep), "l"(b0 + kStep), "l"(a0 + 2 * kStep), "l"(b0 + 2 * kStep), "l"(a0 + 3 * kStep),
+              "l"(b0 + 3 * kStep)
+            : "memory");
+    } else {
+        asm volatile(
+            "{\n .reg .pred p, q;\n .reg .b64 a, b;\n setp.ne.b32 q, %4, 0;\n"
+            " mbarrier.test_wait.parity.shared::cta.b64 p, [%5], %6;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], %2, %3, %7, q;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], %8, %9, %7, 1;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], %10, %11, %7, 1;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], %12, %13, %7, 1;\n"
+            " add.s64 a, %2, %14;\n add.s64 b, %3, %15;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], a, b, %7, 1;\n"
+            " add.s64 a, %8, %14;\n add.s64 b, %9, %15;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], a, b, %7, 1;\n"
+            " add.s64 a, %10, %14;\n add.s64 b, %11, %15;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], a, b, %7, 1;\n"
+            " add.s64 a, %12, %14;\n add.s64 b, %13, %15;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%1], a, b, %7, 1;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(d), "l"(a0), "l"(b0), "r"(accumulate), "r"(next_bar), "r"(parity), "r"(idesc),
+              "l"(a0 + kStep), "l"(b0 + kStep), "l"(a0 + 2 * kStep), "l"(b0 + 2 * kStep), "l"(a0 + 3 * kStep),
+              "l"(b0 + 3 * kStep), "l"(aBlk), "l"(bBlk)
+            : "memory");
+    }
+    return ok != 0;
+}
+
 __device__ __forceinline__ void raise_abort(const TcGemmParams &p, volatile int *abort_flag, int code) {
     atomicCAS(p.status, 0, code);
     *abort_flag = 1;
@@ -220,110 +282,134 @@ __global__ void __launch_bounds__(THREADS, 1)
             ptx::tma_prefetch_desc(&tmB);
             int stage = 0;
             uint32_t phase = 0;
-            bool issued[STAGES];
-            uint32_t issued_phase[STAGES];
-            for (int i = 0; i < STAGES; i++) {
-                issued[i] = false;
-                issued_phase[i] = 0;
-            }
+            int issued = 0; // slots that have received a group (they fill in order 0, 1, 2)
             bool ok = true;
             for (int tile = cta0; tile < total_tiles && ok; tile += ctas) {
                 const TileJob job = resolve<GROUPED, CL>(p, items, work, tile, crank);
                 for (int d = 0; d < S && ok; d++) {
-                    const int kbs = (d + 1) * job.nkb;
-                    for (int j = 0; j < kbs; j++) {
-                        const int s = j / job.nkb, kb = j - s * job.nkb, t = d - s;
-                        const long long t0 = p.prof ? clock64() : 0;
-                        const bool got = ptx::mbar_wait(&empty[stage], phase ^ 1, p.timeout_ns, abort_flag);
-                        if (p.prof) prof_add(p, kProfProducerWaitEmpty, clock64() - t0);
-                        if (!got) {
-                            raise_abort(p, abort_flag, 1);
-                            ok = false;
-                            break;
-                        }
-                        ptx::mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
-                        const int kc = (p.kb0 + kb) * kBK;
-                        uint8_t *sa = smem + stage * STAGE_BYTES;
-                        ptx::tma_load_3d(sa, &tmA, &full[stage], kc, job.mt * kBM, job.zA + s);
-                        if (CL == 1) {
-                            ptx::tma_load_3d(sa + A_BYTES, &tmB, &full[stage], kc, job.nt * kBN, job.zB + t);
-                        } else {
-                            // this CTA's half of the shared B tile, written into both CTAs
-                            ptx::tma_load_3d_mc(sa + A_BYTES + crank * (B_BYTES / CL), &tmBh, &full[stage], kc,
-                                                job.nt * kBN + (int)crank * (kBN / CL), job.zB + t,
-                                                (uint16_t)((1u << CL) - 1));
-                        }
-                        issued[stage] = true;
-                        issued_phase[stage] = phase;
-                        if (++stage == STAGES) {
-                            stage = 0;
-                            phase ^= 1;
+                    for (int s = 0; s <= d && ok; s++) {
+                        const int t = d - s;
+                        for (int kb = 0; kb < job.nkb; kb += GROUP_KB) {
+                            const long long t0 = p.prof ? clock64() : 0;
+                            const bool got = ptx::mbar_wait(&empty[stage], phase ^ 1, p.timeout_ns, abort_flag);
+                            if (p.prof) prof_add(p, kProfProducerWaitEmpty, clock64() - t0);
+                            if (!got) {
+                                raise_abort(p, abort_flag, 1);
+                                ok = false;
+                                break;
+                            }
+                            ptx::mbar_arrive_expect_tx(&full[stage], (uint32_t)STAGE_BYTES);
+                            uint8_t *sa = smem + stage * STAGE_BYTES;
+#pragma unroll
+                            for (int h = 0; h < GROUP_KB; h++) {
+                                const int kc = (p.kb0 + kb + h) * kBK;
+                                ptx::tma_load_3d(sa + h * A_BYTES, &tmA, &full[stage], kc, job.mt * kBM, job.zA + s);
+                                uint8_t *sb = sa + GROUP_KB * A_BYTES + h * B_BYTES;
+                                if (CL == 1) {
+                                    ptx::tma_load_3d(sb, &tmB, &full[stage], kc, job.nt * kBN, job.zB + t);
+                                } else {
+                                    // this CTA's half of the shared B tile, written into both CTAs
+                                    ptx::tma_load_3d_mc(sb + crank * (B_BYTES / CL), &tmBh, &full[stage], kc,
+                                                        job.nt * kBN + (int)crank * (kBN / CL), job.zB + t,
+                                                        (uint16_t)((1u << CL) - 1));
+                                }
+                            }
+                            if (issued < STAGES) issued++;
+                            if (++stage == STAGES) {
+                                stage = 0;
+                                phase ^= 1;
+                            }
                         }
                     }
                 }
             }
-            // Every load issued must land before the CTA may exit.
-            for (int i = 0; i < STAGES; i++)
-                if (issued[i] && !ptx::mbar_wait(&full[i], issued_phase[i], DRAIN_NS, nullptr))
+            // Slot i last received a group in the current round of the ring if
+            // i < stage, else in the previous one.
+            for (int i = 0; i < issued; i++)
+                if (!ptx::mbar_wait(&full[i], i < stage ? phase : phase ^ 1, DRAIN_NS, nullptr))
                     raise_abort(p, abort_flag, 4);
         }
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
             const uint32_t idesc = ptx::idesc_bf16_f32(kBM, kBN);
-            int stage = 0;
+            const uint32_t smem_base = ptx::smem_u32(smem), full_base = ptx::smem_u32(full);
+            // Descriptors of the three slots, fixed for the whole kernel: the issue
+            // loop below is unrolled over the slots so that none is recomputed.
+            const uint64_t da0 = ptx::smem_desc_sw128(smem_base), db0 = ptx::smem_desc_sw128(smem_base + 2 * A_BYTES);
+            const uint64_t da1 = ptx::smem_desc_sw128(smem_base + STAGE_BYTES),
+                           db1 = ptx::smem_desc_sw128(smem_base + STAGE_BYTES + 2 * A_BYTES);
+            const uint64_t da2 = ptx::smem_desc_sw128(smem_base + 2 * STAGE_BYTES),
+                           db2 = ptx::smem_desc_sw128(smem_base + 2 * STAGE_BYTES + 2 * A_BYTES);
             uint32_t phase = 0;
             int abuf = 0;
             uint32_t aphase = 0;
-            bool ok = true;
-            for (int tile = cta0; tile < total_tiles && ok; tile += ctas) {
-                const int nkb = GROUPED ? items[work[tile].x].nkb : p.nkb;
-                for (int d = 0; d < S && ok; d++) {
-                    const int kbs = (d + 1) * nkb;
-                    for (int c0 = 0; c0 < kbs && ok; c0 += kChunkKB) {
-                        const int c1 = min(c0 + kChunkKB, kbs);
-                        const long long ta = p.prof ? clock64() : 0;
-                        const bool got_acc = ptx::mbar_wait(&acce[abuf], aphase ^ 1, p.timeout_ns, abort_flag);
-                        if (p.prof) prof_add(p, kProfMmaWaitAcc, clock64() - ta);
-                        if (!got_acc) {
-                            raise_abort(p, abort_flag, 2);
-                            ok = false;
-                            break;
-                        }
-                        ptx::tc_fence_after();
-                        const uint32_t dt = tmem + (uint32_t)(abuf * kBN);
-                        for (int j = c0; j < c1; j++) {
-                            const long long tf = p.prof ? clock64() : 0;
-                            const bool got_full = ptx::mbar_wait(&full[stage], phase, p.timeout_ns, abort_flag);
-                            if (p.prof) prof_add(p, kProfMmaWaitFull, clock64() - tf);
-                            if (!got_full) {
-                                raise_abort(p, abort_flag, 2);
-                                ok = false;
-                                break;
-                            }
-                            ptx::tc_fence_after();
-                            const uint32_t sa = ptx::smem_u32(smem + stage * STAGE_BYTES);
-                            const uint32_t sb = sa + A_BYTES;
-#pragma unroll
-                            for (int k = 0; k < kBK / 16; k++)
-                                ptx::mma_bf16(dt, ptx::smem_desc_sw128(sa + k * 32), ptx::smem_desc_sw128(sb + k * 32),
-                                              idesc, (j > c0 || k > 0) ? 1u : 0u);
-                            if (CL == 1)
-                                ptx::mma_commit(&empty[stage]);
-                            else
-                                ptx::mma_commit_mc(&empty[stage], (uint16_t)((1u << CL) - 1));
-                            if (++stage == STAGES) {
-                                stage = 0;
-                                phase ^= 1;
-                            }
-                        }
-                        if (!ok) break;
-                        ptx::mma_commit(&accf[abuf]);
-                        abuf ^= 1;
-                        if (abuf == 0) aphase ^= 1;
+            bool ready = false; // the look-ahead test saw the next slot full
+            uint32_t dt = tmem;
+            // Position in the group sequence: tile, slice group d, pair s, group g
+            // of the pair (gpp groups per pair), groups in the open chunk.
+            int tile = cta0, d = 0, s = 0, g = 0, in_chunk = 0;
+            int gpp = tile < total_tiles ? (GROUPED ? items[work[tile].x].nkb : p.nkb) / GROUP_KB : 0;
+            auto close_chunk = [&]() {
+                ptx::mma_commit(&accf[abuf]);
+                abuf ^= 1;
+                if (abuf == 0) aphase ^= 1;
+                in_chunk = 0;
+            };
+            // One group in ring slot ST; false when the sequence ended or a wait gave up.
+            auto step = [&](auto slot) -> bool {
+                constexpr int ST = decltype(slot)::value;
+                if (in_chunk == 0) {
+                    const long long ta = p.prof ? clock64() : 0;
+                    const bool got_acc = ptx::mbar_wait(&acce[abuf], aphase ^ 1, p.timeout_ns, abort_flag);
+                    if (p.prof) prof_add(p, kProfMmaWaitAcc, clock64() - ta);
+                    if (!got_acc) {
+                        raise_abort(p, abort_flag, 2);
+                        return false;
+                    }
+                    dt = tmem + (uint32_t)(abuf * kBN);
+                }
+                if (!ready) {
+                    const long long tf = p.prof ? clock64() : 0;
+                    const bool got_full = ptx::mbar_wait(&full[ST], phase, p.timeout_ns, abort_flag);
+                    if (p.prof) prof_add(p, kProfMmaWaitFull, clock64() - tf);
+                    if (!got_full) {
+                        raise_abort(p, abort_flag, 2);
+                        return false;
                     }
                 }
-            }
+                ptx::tc_fence_after();
+                const uint64_t da = ST == 0 ? da0 : (ST == 1 ? da1 : da2);
+                const uint64_t db = ST == 0 ? db0 : (ST == 1 ? db1 : db2);
+                const uint32_t nphase = ST == STAGES - 1 ? phase ^ 1 : phase;
+                ready = mma_group<2>(dt, da, db, idesc, in_chunk > 0 ? 1u : 0u,
+                                     full_base + (uint32_t)(((ST + 1) % STAGES) * 8), nphase);
+                if (CL == 1)
+                    ptx::mma_commit(&empty[ST]);
+                else
+                    ptx::mma_commit_mc(&empty[ST], (uint16_t)((1u << CL) - 1));
+                phase = nphase;
+                if (++in_chunk == kChunkKB / GROUP_KB) close_chunk();
+                if (++g == gpp) {
+                    g = 0;
+                    if (++s > d) {
+                        s = 0;
+                        if (in_chunk > 0) close_chunk(); // the slice group ends inside a chunk
+                        if (++d == S) {
+                            d = 0;
+                            tile += ctas;
+                            if (tile >= total_tiles) return false;
+                            gpp = (GROUPED ? items[work[tile].x].nkb : p.nkb) / GROUP_KB;
+                        }
+                    }
+                }
+                return true;
+            };
+            static_assert(STAGES == 3, "the issue loop is unrolled over three slots");
+            if (gpp > 0)
+                while (step(std::integral_constant<int, 0>{}) && step(std::integral_constant<int, 1>{}) &&
+                       step(std::integral_constant<int, 2>{})) {
+                }
             // All issued MMAs must complete before TMEM is released.
             ptx::mma_commit(done);
             if (!ptx::mbar_wait(done, 0, DRAIN_NS, nullptr)) raise_abort(p, abort_flag, 5);
