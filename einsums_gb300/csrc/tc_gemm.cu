@@ -14,11 +14,12 @@
 //               without blocking in the same instruction sequence as the
 //               current group's MMAs and waits only when that test failed;
 //   warps 2-9   epilogue (two warps per TMEM lane quadrant, 64 columns each):
-//               after every chunk of <= 1024 products per output,
-//               convert the exact FP32 sums to int64 and accumulate them in
-//               TMEM (columns 256..511 hold the low and high words), then at
-//               the end of a tile scale by 2^(eA+eB-...) in FP64 and apply
-//               C = cp*C + ab*v through the output's index map.
+//               after every chunk of <= 1024 products per output, convert the
+//               exact FP32 sums to integers and add them to int32 partial
+//               sums in registers, folded into an int64 part in TMEM at the
+//               end of each slice group; at the end of a tile scale by
+//               2^(eA+eB-...) in FP64 and apply C = cp*C + ab*v through the
+//               output's index map.
 // TMEM columns: [0,128) accumulator 0, [128,256) accumulator 1,
 //               [256,384) int64 low words, [384,512) int64 high words.
 // Every mbarrier wait is bounded (split.cuh, ptx.cuh): on a timeout the CTA
@@ -46,6 +47,7 @@ constexpr uint32_t TMEM_COLS = 512;
 constexpr int AUX_BYTES = 256;
 constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + AUX_BYTES + 4 * kBN * (8 + 4);  // 8 warps x 64 columns
 constexpr int GROUP_M = 16; // tile rasterisation: groups of 16 row tiles share B tiles in L2
+constexpr int kFinCols = 4;  // columns of the pending tile finished per batch
 constexpr unsigned long long DRAIN_NS = 200ull * 1000 * 1000;
 
 // Optional cycle counters per CTA (TcGemmParams::prof, 8 slots per CTA).
@@ -440,18 +442,18 @@ __global__ void __launch_bounds__(THREADS, 1)
         int64_t pend_rowOff = 0;
         auto finalize_cols = [&](int upto) {
             if (pend && pend_row_ok) {
-                for (int c0 = pend_done; c0 < upto; c0 += 8) {
-                    long long Rv[8];
-                    double old[8];
+                for (int c0 = pend_done; c0 < upto; c0 += kFinCols) {
+                    long long Rv[kFinCols];
+                    double old[kFinCols];
 #pragma unroll
-                    for (int i = 0; i < 8; i++) Rv[i] = rb[c0 + i];
+                    for (int i = 0; i < kFinCols; i++) Rv[i] = rb[c0 + i];
                     if (!plain_store) {
 #pragma unroll
-                        for (int i = 0; i < 8; i++)
+                        for (int i = 0; i < kFinCols; i++)
                             old[i] = colExp[c0 + i] != INT_MAX ? pend_C[pend_rowOff + colOff[c0 + i]] : 0.0;
                     }
 #pragma unroll
-                    for (int i = 0; i < 8; i++) {
+                    for (int i = 0; i < kFinCols; i++) {
                         const int ce = colExp[c0 + i];
                         if (ce == INT_MAX) continue;
                         long long R = Rv[i];
@@ -470,19 +472,22 @@ __global__ void __launch_bounds__(THREADS, 1)
             pend_done = upto;
         };
         for (int tile = cta0; tile < total_tiles && ok; tile += ctas) {
-            const TileJob job = resolve<GROUPED, CL>(p, items, work, tile, crank);
-            const int64_t m = (int64_t)job.mt * kBM + row;
-            const bool row_ok = m < job.M;
-            int64_t rowOff = 0;
-            int rowExp = 0;
-            if (row_ok) {
-                int64_t oa, ob;
-                group_offsets32(*job.mg, (uint32_t)m, oa, ob, rowOff);
-                rowExp = job.eA[m];
-            }
-            bool first = true;
+            // Only the K block count is held through the chunks; the rest of the
+            // tile's description is resolved at its end (registers are scarce here).
+            const int nkb = GROUPED ? items[work[tile].x].nkb : p.nkb;
+            // Running sum of this thread's 64 outputs, R = H + L: L (int32, registers)
+            // takes every chunk, H (int64, TMEM columns 256..511) is written only when
+            // L is folded in -- at the end of each slice group (Horner step R *= 256)
+            // and every 64 chunks (|L| < 64 * 2^24 = 2^30).  Keeping the per-chunk
+            // work free of TMEM stores matters: a tcgen05.st from the epilogue warps
+            // that share the MMA issuer's sub-partition stalls the issue.
+            int32_t L[kBN / 2];
+#pragma unroll
+            for (int i = 0; i < kBN / 2; i++) L[i] = 0;
+            bool hvalid = false; // H holds a part of the sum (else it reads as 0)
+            int since_fold = 0;
             for (int d = 0; d < S && ok; d++) {
-                const int kbs = (d + 1) * job.nkb;
+                const int kbs = (d + 1) * nkb;
                 for (int c0 = 0; c0 < kbs; c0 += kChunkKB) {
                     const long long tw = (p.prof && ew == 0 && lane == 0) ? clock64() : 0;
                     bool w = ptx::mbar_wait(&accf[abuf], aphase, p.timeout_ns, abort_flag);
@@ -495,39 +500,53 @@ __global__ void __launch_bounds__(THREADS, 1)
                         break;
                     }
                     ptx::tc_fence_after();
-                    const bool shift = (c0 == 0) && !first;
-#pragma unroll 1
+#pragma unroll
                     for (int cc = 0; cc < kBN / 32; cc++) {
-                        const uint32_t col = (uint32_t)(col0 + cc * 16);
-                        uint32_t acc[16], lo[16], hi[16];
-                        ptx::tmem_ld16(tl + (uint32_t)(abuf * kBN) + col, acc);
-                        if (!first) {
-                            ptx::tmem_ld16(tl + 256u + col, lo);
-                            ptx::tmem_ld16(tl + 384u + col, hi);
-                        }
+                        uint32_t acc[16];
+                        ptx::tmem_ld16(tl + (uint32_t)(abuf * kBN + col0 + cc * 16), acc);
                         ptx::tmem_wait_ld();
 #pragma unroll
-                        for (int i = 0; i < 16; i++) {
-                            const long long x = (long long)__float2int_rn(__uint_as_float(acc[i]));
-                            long long R = first ? 0ll : (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
-                            if (shift) R *= 256;
-                            R += x;
-                            lo[i] = (uint32_t)((unsigned long long)R);
-                            hi[i] = (uint32_t)((unsigned long long)R >> 32);
-                        }
-                        ptx::tmem_st16(tl + 256u + col, lo);
-                        ptx::tmem_st16(tl + 384u + col, hi);
+                        for (int i = 0; i < 16; i++) L[cc * 16 + i] += __float2int_rn(__uint_as_float(acc[i]));
                     }
-                    ptx::tmem_wait_st();
                     ptx::tc_fence_before();
                     __syncwarp();
                     if (lane == 0) ptx::mbar_arrive(&acce[abuf]);
-                    if (p.prof && ew == 0 && lane == 0) prof_add(p, kProfEpiFlush, clock64() - tw1);
                     abuf ^= 1;
                     if (abuf == 0) aphase ^= 1;
-                    first = false;
+                    // Fold L into H every 64 chunks and at the end of each slice group,
+                    // with the Horner step R *= 256 before the next one; after the last
+                    // slice group H holds the tile's sums and L is free.
+                    const bool group_end = c0 + kChunkKB >= kbs;
+                    const bool shift = group_end && d + 1 < S;
+                    if (++since_fold == 64 || group_end) {
+#pragma unroll
+                        for (int cc = 0; cc < kBN / 16; cc++) {
+                            const uint32_t col = (uint32_t)(col0 + cc * 8);
+                            uint32_t lo[8], hi[8];
+                            if (hvalid) {
+                                ptx::tmem_ld8(tl + 256u + col, lo);
+                                ptx::tmem_ld8(tl + 384u + col, hi);
+                                ptx::tmem_wait_ld();
+                            }
+#pragma unroll
+                            for (int i = 0; i < 8; i++) {
+                                long long H = hvalid ? (long long)(((unsigned long long)hi[i] << 32) | lo[i]) : 0ll;
+                                H += L[cc * 8 + i];
+                                if (shift) H *= 256;
+                                lo[i] = (uint32_t)((unsigned long long)H);
+                                hi[i] = (uint32_t)((unsigned long long)H >> 32);
+                                L[cc * 8 + i] = 0;
+                            }
+                            ptx::tmem_st8(tl + 256u + col, lo);
+                            ptx::tmem_st8(tl + 384u + col, hi);
+                            ptx::tmem_wait_st();
+                        }
+                        hvalid = true;
+                        since_fold = 0;
+                    }
+                    if (p.prof && ew == 0 && lane == 0) prof_add(p, kProfEpiFlush, clock64() - tw1);
                     // a slice of the pending tile while the MMAs run
-                    if (pend_done < kBN / 2) finalize_cols(pend_done + 8);
+                    if (pend_done < kBN / 2) finalize_cols(pend_done + kFinCols);
                 }
             }
             if (!ok) break;
@@ -536,6 +555,16 @@ __global__ void __launch_bounds__(THREADS, 1)
             const long long tfin = (p.prof && ew == 0 && lane == 0) ? clock64() : 0;
             finalize_cols(kBN / 2);
             __syncwarp();
+            const TileJob job = resolve<GROUPED, CL>(p, items, work, tile, crank);
+            const int64_t m = (int64_t)job.mt * kBM + row;
+            const bool row_ok = m < job.M;
+            int64_t rowOff = 0;
+            int rowExp = 0;
+            if (row_ok) {
+                int64_t oa, ob;
+                group_offsets32(*job.mg, (uint32_t)m, oa, ob, rowOff);
+                rowExp = job.eA[m];
+            }
 #pragma unroll 1
             for (int cc = 0; cc < kBN / 32; cc++) {
                 const uint32_t col = (uint32_t)(col0 + cc * 16);
