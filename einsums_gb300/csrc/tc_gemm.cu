@@ -45,9 +45,13 @@ constexpr int STAGE_BYTES = GROUP_KB * KB_BYTES;  // [A kb0][A kb1][B kb0][B kb1
 constexpr int THREADS = 320; // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int AUX_BYTES = 256;
-constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + AUX_BYTES + 4 * kBN * (8 + 4);  // 8 warps x 64 columns
-constexpr int GROUP_M = 16; // tile rasterisation: groups of 16 row tiles share B tiles in L2
 constexpr int kFinCols = 4;  // columns of the pending tile finished per batch
+constexpr int FIN_T = 33;    // padded row count of a warp's transposition buffer
+// per epilogue warp: 64 column offsets and exponents, the transposition buffer
+// of one batch, and its 32 rows' output offsets and validity
+constexpr int EPI_WARP_BYTES = (kBN / 2) * (8 + 4) + kFinCols * FIN_T * 8 + 32 * (8 + 4);
+constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + AUX_BYTES + 8 * EPI_WARP_BYTES + 64;
+constexpr int GROUP_M = 16; // tile rasterisation: groups of 16 row tiles share B tiles in L2
 constexpr unsigned long long DRAIN_NS = 200ull * 1000 * 1000;
 
 // Optional cycle counters per CTA (TcGemmParams::prof, 8 slots per CTA).
@@ -243,7 +247,10 @@ __global__ void __launch_bounds__(THREADS, 1)
     // per-epilogue-warp copies of the tile's column offsets and exponents, so
     // the epilogue warps never wait on one another
     int64_t *colOffAll = (int64_t *)(smem + STAGES * STAGE_BYTES + AUX_BYTES);
-    int *colExpAll = (int *)(colOffAll + 4 * kBN); // 8 warps x 64 columns each
+    int *colExpAll = (int *)(colOffAll + 4 * kBN);             // 8 warps x 64 columns each
+    double *finTAll = (double *)(colExpAll + 4 * kBN);         // 8 warps x kFinCols x FIN_T
+    int64_t *rowOffAll = (int64_t *)(finTAll + 8 * kFinCols * FIN_T); // 8 warps x 32 rows
+    int *rowOkAll = (int *)(rowOffAll + 8 * 32);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long t_start = p.prof ? clock64() : 0;
@@ -426,47 +433,95 @@ __global__ void __launch_bounds__(THREADS, 1)
         const uint32_t tl = tmem + ((uint32_t)(q * 32) << 16);
         int64_t *colOff = colOffAll + ew * (kBN / 2);
         int *colExp = colExpAll + ew * (kBN / 2);
+        double *finT = finTAll + ew * (kFinCols * FIN_T);
+        int64_t *rowOffW = rowOffAll + ew * 32;
+        int *rowOkW = rowOkAll + ew * 32;
         int abuf = 0;
         uint32_t aphase = 0;
         bool ok = true;
         const bool plain_store = p.zero && p.cp == 0.0;
         // The previous ("pending") tile: its int64 sums wait in this CTA's scratch
-        // (this thread's row, 64 columns) and are finished 8 columns at a time
-        // after each flush of the next tile, so the FP64 epilogue never holds
-        // the accumulators the MMA issuer is waiting for.  colOff / colExp
-        // describe the pending tile.
-        long long *const rb = p.rbuf + ((size_t)blockIdx.x * kBM + row) * kBN + col0;
+        // (column-major, so the warp's stores and loads of it are contiguous) and
+        // are finished kFinCols columns at a time after each flush of the next
+        // tile, so the FP64 epilogue never holds the accumulators the MMA issuer
+        // is waiting for.  When C is contiguous along the rows, one thread per
+        // row reads and writes C directly (consecutive lanes, consecutive rows);
+        // otherwise a batch is converted with one thread per row and transposed
+        // through shared memory so that the read-modify-write of C runs along a
+        // row.  colOff / colExp / rowOffW / rowOkW describe the pending tile.
+        long long *const rbc = p.rbuf + (size_t)blockIdx.x * kBM * kBN;
         bool pend = false, pend_row_ok = false;
+        bool pend_rows_fast = false; // C is contiguous along the rows: one thread per row stays coalesced
         int pend_done = 0, pend_rowExp = 0;
         double *pend_C = nullptr;
-        int64_t pend_rowOff = 0;
         auto finalize_cols = [&](int upto) {
-            if (pend && pend_row_ok) {
-                for (int c0 = pend_done; c0 < upto; c0 += kFinCols) {
-                    long long Rv[kFinCols];
-                    double old[kFinCols];
+            if (pend && pend_rows_fast) {
+                if (pend_row_ok) {
+                    const int64_t rowOff = rowOffW[lane];
+                    for (int c0 = pend_done; c0 < upto; c0 += kFinCols) {
+                        long long Rv[kFinCols];
+                        double old[kFinCols];
 #pragma unroll
-                    for (int i = 0; i < kFinCols; i++) Rv[i] = rb[c0 + i];
-                    if (!plain_store) {
+                        for (int i = 0; i < kFinCols; i++) Rv[i] = rbc[(size_t)(col0 + c0 + i) * kBM + row];
+                        if (!plain_store) {
 #pragma unroll
-                        for (int i = 0; i < kFinCols; i++)
-                            old[i] = colExp[c0 + i] != INT_MAX ? pend_C[pend_rowOff + colOff[c0 + i]] : 0.0;
+                            for (int i = 0; i < kFinCols; i++)
+                                old[i] = colExp[c0 + i] != INT_MAX ? pend_C[rowOff + colOff[c0 + i]] : 0.0;
+                        }
+#pragma unroll
+                        for (int i = 0; i < kFinCols; i++) {
+                            const int ce = colExp[c0 + i];
+                            if (ce == INT_MAX) continue;
+                            long long R = Rv[i];
+                            if (p.ab_neg) R = -R;
+                            double v;
+                            if (pend_rowExp == INT_MIN || ce == INT_MIN)
+                                v = __longlong_as_double(0x7ff8000000000000ll);
+                            else
+                                v = int64_times_pow2(R, pend_rowExp + ce + p.shift_const);
+                            if (!p.ab_pow2) v *= p.ab;
+                            pend_C[rowOff + colOff[c0 + i]] =
+                                plain_store ? v : (p.cp == 1.0 ? old[i] + v : fma(p.cp, old[i], v));
+                        }
                     }
+                }
+            } else if (pend) {
+                for (int c0 = pend_done; c0 < upto; c0 += kFinCols) {
 #pragma unroll
                     for (int i = 0; i < kFinCols; i++) {
                         const int ce = colExp[c0 + i];
-                        if (ce == INT_MAX) continue;
-                        long long R = Rv[i];
-                        if (p.ab_neg) R = -R;
-                        double v;
-                        if (pend_rowExp == INT_MIN || ce == INT_MIN)
-                            v = __longlong_as_double(0x7ff8000000000000ll);
-                        else
-                            v = int64_times_pow2(R, pend_rowExp + ce + p.shift_const);
-                        if (!p.ab_pow2) v *= p.ab;
-                        double *cptr = pend_C + pend_rowOff + colOff[c0 + i];
-                        *cptr = plain_store ? v : (p.cp == 1.0 ? old[i] + v : fma(p.cp, old[i], v));
+                        double v = 0.0;
+                        if (pend_row_ok && ce != INT_MAX) {
+                            long long R = rbc[(size_t)(col0 + c0 + i) * kBM + row];
+                            if (p.ab_neg) R = -R;
+                            if (pend_rowExp == INT_MIN || ce == INT_MIN)
+                                v = __longlong_as_double(0x7ff8000000000000ll);
+                            else
+                                v = int64_times_pow2(R, pend_rowExp + ce + p.shift_const);
+                            if (!p.ab_pow2) v *= p.ab;
+                        }
+                        finT[i * FIN_T + lane] = v;
                     }
+                    __syncwarp();
+                    // lanes 4r..4r+3 take the batch's columns of row r (8 rows per pass)
+                    double old[kFinCols];
+                    if (!plain_store) {
+#pragma unroll
+                        for (int k = 0; k < kFinCols; k++) {
+                            const int e = k * 32 + lane, r = e / kFinCols, c = e % kFinCols;
+                            old[k] = (rowOkW[r] && colExp[c0 + c] != INT_MAX) ? pend_C[rowOffW[r] + colOff[c0 + c]] : 0.0;
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < kFinCols; k++) {
+                        const int e = k * 32 + lane, r = e / kFinCols, c = e % kFinCols;
+                        if (rowOkW[r] && colExp[c0 + c] != INT_MAX) {
+                            const double v = finT[c * FIN_T + r];
+                            pend_C[rowOffW[r] + colOff[c0 + c]] =
+                                plain_store ? v : (p.cp == 1.0 ? old[k] + v : fma(p.cp, old[k], v));
+                        }
+                    }
+                    __syncwarp();
                 }
             }
             pend_done = upto;
@@ -574,7 +629,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 ptx::tmem_wait_ld();
 #pragma unroll
                 for (int i = 0; i < 16; i++)
-                    rb[cc * 16 + i] = (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
+                    rbc[(size_t)(col0 + cc * 16 + i) * kBM + row] = (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
             }
             ptx::tc_fence_before();
             for (int i = lane; i < kBN / 2; i += 32) {
@@ -589,11 +644,14 @@ __global__ void __launch_bounds__(THREADS, 1)
                 colExp[i] = ex;
             }
             __syncwarp();
+            rowOffW[lane] = rowOff;
+            rowOkW[lane] = row_ok ? 1 : 0;
+            __syncwarp();
             pend = true;
             pend_done = 0;
             pend_row_ok = row_ok;
+            pend_rows_fast = job.mg->n > 0 && job.mg->s[2][job.mg->n - 1] == 1;
             pend_rowExp = rowExp;
-            pend_rowOff = rowOff;
             pend_C = job.C;
             if (p.prof && ew == 0 && lane == 0) prof_add(p, kProfEpiFinal, clock64() - tfin);
         }
