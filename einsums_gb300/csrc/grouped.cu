@@ -237,18 +237,6 @@ __global__ void __launch_bounds__(TT *TR) k_grouped_rowmax(const GOp *ops, int n
     }
 }
 
-__device__ __forceinline__ void to_digits(double x, int e, int S, int *dig) {
-    const double y = scalbn(x, split::kTopBits + split::kBits * (S - 1) - e);
-    long long F = __double2ll_rn(y);
-    for (int s = S - 1; s >= 1; s--) {
-        int d = (int)(F & 255);
-        if (d > 128) d -= 256;
-        dig[s] = d;
-        F = (F - d) / 256;
-    }
-    dig[0] = (int)F;
-}
-
 __global__ void __launch_bounds__(TT *TR) k_grouped_digits(const GOp *ops, int nops, int64_t total_units,
                                                            const int *rexp, __nv_bfloat16 *planes, int64_t Rmax,
                                                            int64_t Kmaxp, int S) {
@@ -306,7 +294,7 @@ __global__ void __launch_bounds__(TT *TR) k_grouped_digits(const GOp *ops, int n
             if (e == INT_MIN) {
                 for (int s = 0; s < S; s++) dig[s] = 0;
             } else {
-                to_digits(tile[j][tx], e, S, dig);
+                split::to_digits(tile[j][tx], e, S, dig);
             }
             const int64_t z0 = g.zbase + b * S;
             for (int s = 0; s < S; s++)

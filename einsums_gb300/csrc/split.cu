@@ -10,6 +10,7 @@
 // then the tcgen05 GEMM (tc_gemm.cu) over the digit planes.  The operands'
 // index permutation is folded into the address maps of these kernels and of
 // the GEMM epilogue: nothing but the BF16 digit planes is materialised.
+#include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -40,6 +41,10 @@ struct OperandMap {
     int64_t rows, Rp;  // logical and padded rows per batch
     int64_t K, Kp;
     int nbatch;
+    // Element offsets of every row and every k (filled by k_operand_offsets),
+    // or null: then each offset is decomposed mode by mode, which costs integer
+    // divisions per element and made these kernels ALU-bound.
+    const int64_t *offr = nullptr, *offk = nullptr;
 };
 
 __device__ __forceinline__ int64_t comp_of(int comp, int64_t oa, int64_t ob) { return comp == 0 ? oa : ob; }
@@ -49,15 +54,28 @@ __device__ __forceinline__ int64_t off_b(const OperandMap &m, int64_t b) {
     group_offsets(m.bg, b, oa, ob, oc);
     return comp_of(m.comp, oa, ob);
 }
-__device__ __forceinline__ int64_t off_r(const OperandMap &m, int64_t r) {
+__device__ __forceinline__ int64_t decompose_r(const OperandMap &m, int64_t r) {
     int64_t oa, ob, oc;
     group_offsets32(m.rg, (uint32_t)r, oa, ob, oc);
     return comp_of(m.comp, oa, ob);
 }
-__device__ __forceinline__ int64_t off_k(const OperandMap &m, int64_t k) {
+__device__ __forceinline__ int64_t decompose_k(const OperandMap &m, int64_t k) {
     int64_t oa, ob, oc;
     group_offsets32(m.kg, (uint32_t)k, oa, ob, oc);
     return comp_of(m.comp, oa, ob);
+}
+__device__ __forceinline__ int64_t off_r(const OperandMap &m, int64_t r) {
+    return m.offr ? __ldg(m.offr + r) : decompose_r(m, r);
+}
+__device__ __forceinline__ int64_t off_k(const OperandMap &m, int64_t k) {
+    return m.offk ? __ldg(m.offk + k) : decompose_k(m, k);
+}
+
+// Fills the row and k offset tables of an operand.
+__global__ void k_operand_offsets(OperandMap m, int64_t *offr, int64_t *offk) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.rows; i += stride) offr[i] = decompose_r(m, i);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m.K; i += stride) offk[i] = decompose_k(m, i);
 }
 
 constexpr int T = 32, TR = 8;
@@ -116,19 +134,6 @@ __global__ void k_split_exponent(const unsigned long long *rowmax, int *e, int64
             frexp(mx, &ex); // mx = f 2^ex with f in [0.5, 1): |x| <= mx < 2^ex
         e[i] = ex;
     }
-}
-
-// Balanced base-256 digits of x * 2^(7 + 8(S-1) - e), least significant last.
-__device__ __forceinline__ void to_digits(double x, int e, int S, int *dig) {
-    const double y = scalbn(x, kTopBits + kBits * (S - 1) - e);
-    long long F = __double2ll_rn(y);
-    for (int s = S - 1; s >= 1; s--) {
-        int d = (int)(F & 255);
-        if (d > 128) d -= 256;
-        dig[s] = d;
-        F = (F - d) / 256;
-    }
-    dig[0] = (int)F;
 }
 
 __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const double *__restrict__ X, const int *rexp,
@@ -211,9 +216,20 @@ int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 bool is_fast(const ModeGroup &g, int comp) { return g.n > 0 && g.s[comp][g.n - 1] == 1; }
 
-eg_status split_operand(const OperandMap &om, const double *X, unsigned long long *rowmax, int *rexp,
-                        __nv_bfloat16 *planes, int S, cudaStream_t s) {
+eg_status split_operand(OperandMap om, const double *X, unsigned long long *rowmax, int *rexp,
+                        __nv_bfloat16 *planes, int S, cudaStream_t s, int64_t *offr, int64_t *offk) {
     const bool k_fast = is_fast(om.kg, om.comp);
+    if (offr && offk) {
+        const int64_t n = std::max(om.rows, om.K);
+        {
+            LaunchScope ls_("k_operand_offsets", s);
+            k_operand_offsets<<<(int)std::min<int64_t>((n + 255) / 256, (int64_t)num_sms() * 8), 256, 0, s>>>(om, offr,
+                                                                                                            offk);
+        }
+        EG_CHECK_LAUNCH("k_operand_offsets");
+        om.offr = offr;
+        om.offk = offk;
+    }
     const bool r_fast = !k_fast && is_fast(om.rg, om.comp);
     EG_CUDA(cudaMemsetAsync(rowmax, 0, (size_t)om.nbatch * om.Rp * sizeof(unsigned long long), s));
     const int cap = num_sms() * 16;
@@ -268,7 +284,11 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     const size_t offEA = offMaxB + round_up(nb * Np * 8, 256);
     const size_t offEB = offEA + round_up(nb * Mp * 4, 256);
     const size_t offR = offEB + round_up(nb * Np * 4, 256);
-    const size_t total = offR + rbuf_bytes();
+    // offset tables (rows and k of each operand) unless they would be large
+    const bool tables = M + K <= (int64_t(1) << 25) && N + K <= (int64_t(1) << 25);
+    const size_t offTab = offR + rbuf_bytes();
+    const size_t tabBytes = tables ? (size_t)(M + N + 2 * K) * 8 : 0;
+    const size_t total = offTab + tabBytes;
     void *ws = nullptr;
     eg_status st = workspace(s, total, &ws);
     if (st != EG_SUCCESS) return st;
@@ -281,8 +301,11 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
 
     OperandMap oa{c.batch, c.m, c.k, 0, M, Mp, K, Kp, (int)nb};
     OperandMap ob{c.batch, c.n, c.k, 1, N, Np, K, Kp, (int)nb};
-    if ((st = split_operand(oa, c.A, maxA, eA, planesA, S, s)) != EG_SUCCESS) return st;
-    if ((st = split_operand(ob, c.B, maxB, eB, planesB, S, s)) != EG_SUCCESS) return st;
+    int64_t *tab = tables ? (int64_t *)(base + offTab) : nullptr;
+    if ((st = split_operand(oa, c.A, maxA, eA, planesA, S, s, tab, tables ? tab + M : nullptr)) != EG_SUCCESS) return st;
+    if ((st = split_operand(ob, c.B, maxB, eB, planesB, S, s, tables ? tab + M + K : nullptr,
+                            tables ? tab + M + K + N : nullptr)) != EG_SUCCESS)
+        return st;
 
     CUtensorMap tmA, tmB, tmBh;
     if ((st = encode_planes(&tmA, planesA, Kp, Mp, nb * S)) != EG_SUCCESS) return st;

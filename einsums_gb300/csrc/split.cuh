@@ -70,6 +70,47 @@ struct TcItem {
     ModeGroup bg, mg, ng;
 };
 
+// round(x * 2^sh) to nearest, ties to even, for |x| 2^sh < 2^52, built from the
+// IEEE fields with integer operations (the FP64 pipe of this GPU runs about two
+// operations per clock per SM; this is the splitting kernels' inner loop).
+__device__ __forceinline__ long long scaled_round(double x, int sh) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)((bits >> 52) & 0x7ff);
+    unsigned long long mant = bits & 0xFFFFFFFFFFFFFull;
+    int e2; // |x| 2^sh = mant * 2^e2
+    if (ex == 0) {
+        e2 = 1 - 1075 + sh;
+    } else {
+        mant |= 1ull << 52;
+        e2 = ex - 1075 + sh;
+    }
+    unsigned long long q;
+    if (e2 >= 0) {
+        q = mant << (e2 < 11 ? e2 : 11); // not reached while |x| 2^sh < 2^52
+    } else if (e2 < -53) {
+        q = 0; // below 1/2
+    } else {
+        const int r = -e2; // 1..53
+        q = mant >> r;
+        const unsigned long long rem = mant & ((1ull << r) - 1), half = 1ull << (r - 1);
+        if (rem > half || (rem == half && (q & 1ull))) q++;
+    }
+    return (bits >> 63) ? -(long long)q : (long long)q;
+}
+
+// Balanced base-256 digits of x * 2^(7 + 8(S-1) - e) rounded to an integer,
+// most significant first: dig[0] in [-128, 128], the others in [-127, 128].
+__device__ __forceinline__ void to_digits(double x, int e, int S, int *dig) {
+    long long F = scaled_round(x, kTopBits + kBits * (S - 1) - e);
+    for (int s = S - 1; s >= 1; s--) {
+        int d = (int)(F & 255);
+        if (d > 128) d -= 256;
+        dig[s] = d;
+        F = (F - d) >> 8; // exact: F - d is a multiple of 256
+    }
+    dig[0] = (int)F;
+}
+
 // Sets the kernels' shared-memory attribute once (call outside stream capture).
 eg_status ensure_tc_attributes();
 // tmBh: the B planes with a 64-row box (half a tile), used when two CTAs of a
