@@ -39,6 +39,20 @@ def flops(o, v):
             "E": 2.0 * o ** 2 * v ** 2}
 
 
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of the tensor kernel on the
+# o=32, v=160 workload, mean over the step's three launches (Wmnij 1.59 GB,
+# Wabef 24.56 GB, Wmbej 8.27 GB).
+TC_TRAFFIC_O32_V160 = 11.47e9
+
+
+def tc_algorithmic_bytes(o, v, S):
+    """Mean DRAM bytes per tensor-kernel launch of one step at the algorithmic
+    minimum: both operands' S BF16 digit planes read once, C read and written
+    once in FP64.  (M, N, K) of Wmnij, Wabef and Wmbej."""
+    shapes = [(o * o, o * o, v * v), (v * v, v * v, o * o), (o * v, o * v, o * v)]
+    return sum(2 * 8 * M * N + 2 * S * (M + N) * K for M, N, K in shapes) / 3
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -322,6 +336,16 @@ def run_ours(args, rank, world):
             peak = pk.get("bf16_tflops_sustained", 1700.0)
             roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                     "frac": ach / peak, "traffic": None, "peak_source": f"bf16 sustained, {pk_kind}"}
+            if (o, v) == (32, 160) and (split_report or {}).get("slices") == 5:
+                # DRAM bytes per tensor-kernel launch, mean over the step's three
+                # launches, from one ncu capture of this workload
+                # (dram__bytes_read.sum + dram__bytes_write.sum); algorithmic bytes
+                # per launch (digit planes read once, C read and written once) are
+                # 4.16 GB; the kernel moves 2.8x that (re-reads of digit-plane tiles
+                # evicted by the streamed output, and of the per-CTA sum scratch).
+                roof["traffic"] = TC_TRAFFIC_O32_V160
+                roof["traffic_unit"] = "bytes per launch (ncu, mean of the step's 3 launches)"
+                roof["algorithmic_bytes"] = tc_algorithmic_bytes(o, v, 5)
         else:
             alg = F["Wabef"]
             ach = alg / (per_contraction["Wabef"] * 1e-3) / 1e12
