@@ -195,6 +195,13 @@ eg_status eg_memory_in_use(size_t *bytes);
  * kernels have no bounded waits). */
 eg_status eg_stream_status(void *stream, int32_t *device_code);
 
+/* Failure-path self-test of the bounded device waits: enqueues on `stream` a kernel that
+ * allocates tensor memory, waits on a barrier nothing arrives on until `limit_ns`
+ * (0 < limit_ns <= 2e9) passes, records a code for eg_stream_status, frees the tensor memory
+ * and returns -- the steps the tensor-core pipeline takes when one of its waits gives up.
+ * No reference counterpart. */
+eg_status eg_selftest_wait_timeout(uint64_t limit_ns, void *stream);
+
 /* Host<->device copies on `stream` (DeviceTensor::read / operator= in DeviceTensor.hpp). */
 eg_status eg_copy_to_device(void *dst, const void *src, size_t bytes, void *stream);
 eg_status eg_copy_to_host(void *dst, const void *src, size_t bytes, void *stream);

@@ -98,6 +98,9 @@ def test_bad_arguments_return_status(lib):
     # permute with a too-small output
     st = lib.eg_permute(0.0, _lib.labels("i"), ctypes.byref(C), 1.0, _lib.labels("i"), ctypes.byref(A), None)
     assert st == 3
+    # the wait self-test refuses limits outside (0, 2 s] before touching the device
+    assert lib.eg_selftest_wait_timeout(0, None) == 1
+    assert lib.eg_selftest_wait_timeout(3_000_000_000, None) == 1
 
 
 def test_memory_budget_refuses(lib):
