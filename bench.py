@@ -518,7 +518,9 @@ def suite_fock(eg, n=100):
         F.zero_()
         eg.einsum(0.0, "pq", F, 2.0, "pqrs", g, "rs", D, precision=prec)
         algK = eg.einsum(1.0, "pq", F, -1.0, "prqs", g, "rs", D, precision=prec)
-        out[prec] = {"J_ms": msJ, "K_ms": msK, "J_alg": algJ, "K_alg": algK,
+        # J and K are GEMV-shaped (N = 1): a split request runs the FP64 kernels (0 slices reported)
+        slices = eg.last_split_report()["slices"]
+        out[prec] = {"J_ms": msJ, "K_ms": msK, "J_alg": algJ, "K_alg": algK, "split_slices": slices,
                      "J_tflops": flop / msJ / 1e9, "K_tflops": flop / msK / 1e9,
                      "J_gbs": 8.0 * n ** 4 / msJ / 1e6, "K_gbs": 8.0 * n ** 4 / msK / 1e6,
                      "F": F.cpu().numpy().copy()}

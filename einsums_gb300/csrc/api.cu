@@ -335,7 +335,13 @@ eg_status einsum_impl(double cp, const int32_t *Cl, const eg_tensor *C, double a
     }
 
     const bool has_k = c.k.n > 0 || c.k.total == 0;
-    if (opt.precision == EG_PRECISION_SPLIT_BF16 && c.k.total > 0 && (c.m.n > 0 || c.n.n > 0)) {
+    // The split form pays for splitting both operands (each read twice, S BF16
+    // planes written) and pads M and N to 128-row tiles.  When M or N is at most
+    // kSplitMinMN (GEMV-shaped products) the FP64 kernels are faster as well as
+    // exact to FP64, so they run instead and the split report shows 0 slices.
+    constexpr int64_t kSplitMinMN = 4;
+    if (opt.precision == EG_PRECISION_SPLIT_BF16 && c.k.total > 0 && c.m.total > kSplitMinMN &&
+        c.n.total > kSplitMinMN) {
         eg_split_report rep{};
         st = launch_split_contract(c, opt.slices, stream, &rep);
         if (st == EG_SUCCESS) set_split_report(rep);

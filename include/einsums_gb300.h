@@ -49,7 +49,9 @@ typedef enum eg_algorithm {
 
 typedef enum eg_precision {
     EG_PRECISION_FP64 = 0,      /* plain FP64 kernels */
-    EG_PRECISION_SPLIT_BF16 = 1 /* FP64 operands split into exponent-scaled BF16 slices on tcgen05 */
+    EG_PRECISION_SPLIT_BF16 = 1 /* FP64 operands split into exponent-scaled BF16 slices on tcgen05; products
+                                 * whose M or N extent is at most 4 (GEMV and DOT shapes) run the FP64
+                                 * kernels instead, which are faster for them, and report 0 slices */
 } eg_precision;
 
 typedef enum eg_semantics {

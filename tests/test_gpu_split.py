@@ -95,6 +95,25 @@ def test_batched_pattern_and_gemv_shape(eg):
     assert err < TOL_SPLIT, err
 
 
+def test_gemv_shapes_run_fp64(eg):
+    # M or N at most 4: the FP64 kernels run (report: 0 slices), bitwise equal to precision="fp64"
+    rng = np.random.default_rng(9)
+    for dims in ({"i": 3, "j": 500, "k": 700}, {"i": 400, "j": 4, "k": 300}):
+        A = cu(rng.standard_normal((dims["i"], dims["k"])))
+        B = cu(rng.standard_normal((dims["k"], dims["j"])))
+        outs = []
+        for prec in ("split_bf16", "fp64"):
+            C = torch.zeros((dims["i"], dims["j"]), dtype=torch.float64, device="cuda")
+            eg.einsum(0.0, "ij", C, 1.0, "ik", A, "kj", B, precision=prec)
+            outs.append(C.cpu().numpy())
+            if prec == "split_bf16":
+                assert eg.last_split_report()["slices"] == 0
+        assert np.array_equal(outs[0], outs[1])
+    # one above the limit takes the split form
+    err, rep = run_case(eg, "ij", "ik", "kj", {"i": 5, "j": 300, "k": 400})
+    assert rep["slices"] == 5 and err < TOL_SPLIT, err
+
+
 def test_rows_with_wide_dynamic_range(eg):
     err, _ = run_case(eg, "ij", "ik", "kj", {"i": 150, "j": 140, "k": 300}, scale_rows=True)
     assert err < TOL_SPLIT, err
