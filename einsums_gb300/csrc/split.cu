@@ -80,27 +80,30 @@ __global__ void k_operand_offsets(OperandMap m, int64_t *offr, int64_t *offk) {
 
 constexpr int T = 32, TR = 8;
 
-// Tiles of 32 rows x 32 k; row_fast: the operand is contiguous along rows.
-__global__ void __launch_bounds__(T *TR) k_split_rowmax(OperandMap m, const double *__restrict__ X,
-                                                        unsigned long long *rowmax, int row_fast) {
+// Work units of 32 rows x kchunk k (kchunk a multiple of T), the k loop inside
+// the unit so that the unit's decomposition, batch offset and row offsets are
+// paid once per unit; one atomicMax per row per unit.  row_fast: the operand is
+// contiguous along rows (lanes walk rows), else along k (lanes walk k).
+__global__ void __launch_bounds__(T *TR, 5) k_split_rowmax(OperandMap m, const double *__restrict__ X,
+                                                        unsigned long long *rowmax, int row_fast, int kchunk) {
     __shared__ unsigned long long red[TR][T];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int64_t rt = (m.rows + T - 1) / T, kt = (m.K + T - 1) / T;
-    const int64_t work = (int64_t)m.nbatch * rt * kt;
-    for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
-        const int64_t ktile = w % kt, rtile = (w / kt) % rt, b = w / (kt * rt);
+    const int64_t rt = (m.rows + T - 1) / T, kcs = (m.K + kchunk - 1) / kchunk;
+    const int64_t units = (int64_t)m.nbatch * rt * kcs;
+    for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+        const int64_t kc = u % kcs, rtile = (u / kcs) % rt, b = u / (kcs * rt);
         const int64_t ob = off_b(m, b);
-        const int64_t r0 = rtile * T, k0 = ktile * T;
-        unsigned long long mx = 0;
+        const int64_t r0 = rtile * T;
+        const int64_t kbeg = kc * kchunk, kend = min(m.K, kbeg + kchunk);
         if (row_fast) {
-            // thread (tx, ty): row r0+tx, k = k0+ty, +8, ...
+            // thread (tx, ty): row r0+tx, k = kbeg+ty, +8, ...
             const int64_t r = r0 + tx;
+            unsigned long long mx = 0;
             if (r < m.rows) {
-                const int64_t orow = ob + off_r(m, r);
-                for (int j = ty; j < T; j += TR) {
-                    const int64_t k = k0 + j;
-                    if (k < m.K) mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(X + orow + off_k(m, k)))));
-                }
+                const double *xr = X + ob + off_r(m, r);
+#pragma unroll 4
+                for (int64_t k = kbeg + ty; k < kend; k += TR)
+                    mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(xr + off_k(m, k)))));
             }
             red[ty][tx] = mx;
             __syncthreads();
@@ -110,14 +113,28 @@ __global__ void __launch_bounds__(T *TR) k_split_rowmax(OperandMap m, const doub
             }
             __syncthreads();
         } else {
-            // thread (tx, ty): k = k0+tx, rows r0+ty, +8, ...; warp reduce along k
-            const int64_t k = k0 + tx;
-            const int64_t ok = k < m.K ? off_k(m, k) : 0;
-            for (int j = ty; j < T; j += TR) {
-                const int64_t r = r0 + j;
-                unsigned long long v = 0;
-                if (r < m.rows && k < m.K) v = (unsigned long long)__double_as_longlong(fabs(__ldg(X + ob + off_r(m, r) + ok)));
+            // thread (tx, ty): rows r0+ty, +8, ...; k = kbeg+tx, +32, ...; warp reduce along k
+            constexpr int RPT = T / TR;
+            const double *xr[RPT];
+            unsigned long long mx[RPT];
+#pragma unroll
+            for (int j = 0; j < RPT; j++) {
+                const int64_t r = r0 + ty + TR * j;
+                xr[j] = r < m.rows ? X + ob + off_r(m, r) : nullptr;
+                mx[j] = 0;
+            }
+#pragma unroll 2
+            for (int64_t k = kbeg + tx; k < kend; k += T) {
+                const int64_t okk = off_k(m, k);
+#pragma unroll
+                for (int j = 0; j < RPT; j++)
+                    if (xr[j]) mx[j] = max(mx[j], (unsigned long long)__double_as_longlong(fabs(__ldg(xr[j] + okk))));
+            }
+#pragma unroll
+            for (int j = 0; j < RPT; j++) {
+                unsigned long long v = mx[j];
                 for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+                const int64_t r = r0 + ty + TR * j;
                 if (tx == 0 && r < m.rows && v) atomicMax(rowmax + b * m.Rp + r, v);
             }
         }
@@ -136,6 +153,9 @@ __global__ void k_split_exponent(const unsigned long long *rowmax, int *e, int64
     }
 }
 
+// 32x32 tiles staged through shared memory so that the operand is read along its
+// contiguous mode and the digit planes are written along k; padding rows and
+// columns are written as 0.
 __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const double *__restrict__ X, const int *rexp,
                                                         __nv_bfloat16 *planes, int S, int row_fast) {
     __shared__ double tile[T][T + 1];
@@ -180,6 +200,13 @@ __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const doub
         }
         __syncthreads();
     }
+}
+
+// K chunk (a multiple of T) giving about eight work units per SM.
+int chunk_for(int64_t units_per_chunk_row, int64_t ktiles) {
+    const int64_t target = (int64_t)num_sms() * 8;
+    const int64_t per_unit = std::max<int64_t>(1, (units_per_chunk_row * ktiles + target - 1) / target);
+    return (int)(std::min<int64_t>(per_unit, ktiles) * T);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -232,12 +259,14 @@ eg_status split_operand(OperandMap om, const double *X, unsigned long long *rowm
     }
     const bool r_fast = !k_fast && is_fast(om.rg, om.comp);
     EG_CUDA(cudaMemsetAsync(rowmax, 0, (size_t)om.nbatch * om.Rp * sizeof(unsigned long long), s));
-    const int cap = num_sms() * 16;
+    const int cap = num_sms() * 8;
     {
-        const int64_t work = (int64_t)om.nbatch * ((om.rows + T - 1) / T) * ((om.K + T - 1) / T);
+        const int64_t rows_units = (int64_t)om.nbatch * ((om.rows + T - 1) / T);
+        const int kchunk = chunk_for(rows_units, (om.K + T - 1) / T);
+        const int64_t work = rows_units * ((om.K + kchunk - 1) / kchunk);
         const int grid = (int)(work < cap ? (work < 1 ? 1 : work) : cap);
         LaunchScope ls_("k_split_rowmax", s);
-        k_split_rowmax<<<grid, dim3(T, TR), 0, s>>>(om, X, rowmax, r_fast ? 1 : 0);
+        k_split_rowmax<<<grid, dim3(T, TR), 0, s>>>(om, X, rowmax, r_fast ? 1 : 0, kchunk);
     }
     EG_CHECK_LAUNCH("k_split_rowmax");
     {
@@ -248,7 +277,7 @@ eg_status split_operand(OperandMap om, const double *X, unsigned long long *rowm
     EG_CHECK_LAUNCH("k_split_exponent");
     {
         const int64_t work = (int64_t)om.nbatch * (om.Rp / T) * (om.Kp / T);
-        const int grid = (int)(work < cap ? work : cap);
+        const int grid = (int)(work < 2 * cap ? work : 2 * cap);
         LaunchScope ls_("k_split_digits", s);
         k_split_digits<<<grid, dim3(T, TR), 0, s>>>(om, X, rexp, planes, S, r_fast ? 1 : 0);
     }
