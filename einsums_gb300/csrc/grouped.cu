@@ -663,6 +663,8 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     }
     p.status = status;
     p.timeout_ns = 2000ull * 1000 * 1000;
+    p.ksplit = 1; // no K slicing in grouped launches
+    p.kslice = 0;
     p.rbuf = (long long *)rbuf;
 
     const int cap = num_sms() * 16;

@@ -317,7 +317,14 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     const bool tables = M + K <= (int64_t(1) << 25) && N + K <= (int64_t(1) << 25);
     const size_t offTab = offR + rbuf_bytes();
     const size_t tabBytes = tables ? (size_t)(M + N + 2 * K) * 8 : 0;
-    const size_t total = offTab + tabBytes;
+    // K slices in parallel when the output has fewer tiles than half the SMs
+    const int64_t tiles = nb * (Mp / kBM) * (Np / kBN);
+    const bool kslicing = tiles < num_sms() / 2;
+    const size_t offRacc = round_up((int64_t)(offTab + tabBytes), 256);
+    const size_t raccBytes = kslicing ? (size_t)tiles * kBM * kBN * 8 : 0;
+    const size_t offRcnt = offRacc + raccBytes;
+    const size_t rcntBytes = kslicing ? (size_t)tiles * 8 * sizeof(int) : 0;
+    const size_t total = offRcnt + rcntBytes;
     void *ws = nullptr;
     eg_status st = workspace(s, total, &ws);
     if (st != EG_SUCCESS) return st;
@@ -368,6 +375,8 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     p.status = status;
     p.timeout_ns = 2000ull * 1000 * 1000;
     p.rbuf = (long long *)(base + offR);
+    p.racc = kslicing ? (long long *)(base + offRacc) : nullptr;
+    p.rcnt = kslicing ? (int *)(base + offRcnt) : nullptr;
 
     // K passes small enough for the exact int64 accumulator; later passes add into C.
     const int64_t kpass = max_k_per_pass(S);
@@ -377,6 +386,20 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     for (int64_t kb0 = 0; kb0 < nkb_total || kb0 == 0; kb0 += kb_per_pass) {
         p.kb0 = (int)kb0;
         p.nkb = (int)std::min<int64_t>(kb_per_pass, nkb_total - kb0);
+        // slices of at least 16 K blocks (one exact chunk), about one work entry per SM
+        p.ksplit = 1;
+        p.kslice = p.nkb;
+        if (kslicing && p.nkb >= 32) {
+            const int want = (int)std::min<int64_t>(num_sms() / tiles, p.nkb / 16);
+            if (want > 1) {
+                p.kslice = (int)round_up((p.nkb + want - 1) / want, kKStep / kBK);
+                p.ksplit = (p.nkb + p.kslice - 1) / p.kslice;
+            }
+        }
+        if (p.ksplit > 1) {
+            EG_CUDA(cudaMemsetAsync(p.racc, 0, raccBytes, s));
+            EG_CUDA(cudaMemsetAsync(p.rcnt, 0, rcntBytes, s));
+        }
         const bool first = kb0 == 0;
         p.cp = first ? c.cp : 1.0;
         p.zero = first ? (c.zero_when_cp_zero ? 1 : 0) : 0;

@@ -55,6 +55,15 @@ struct TcGemmParams {
     // Per-CTA scratch of gridDim.x * 128 * 128 int64: a finished tile's sums
     // wait here until the epilogue converts them during the next tile.
     long long *rbuf;
+    // K slices run in parallel when there are few output tiles: entry t of the
+    // schedule is K slice t % ksplit (kslice K blocks, even; the last slice takes
+    // the rest) of tile t / ksplit.  The slices' exact int64 sums are added into
+    // racc ([tile][128 columns][128 rows]) and the last slice to arrive at a
+    // region of an epilogue warp (counted in rcnt, [tile][8]) finishes it.  Both
+    // are zeroed by the host before the launch; unused when ksplit == 1.
+    int ksplit, kslice;
+    long long *racc;
+    int *rcnt;
 };
 
 // One item of a grouped launch: an independent contraction whose digit planes

@@ -80,7 +80,9 @@ __device__ __forceinline__ void tile_coords(const TcGemmParams &p, int t, int &b
 struct TileJob {
     int mt, nt;
     int zA, zB;  // digit plane of slice 0 for A / B
+    int kbeg;    // first K block (of this pass) of the K slice
     int nkb;     // K blocks
+    int tid;     // linear output tile index (single-contraction form)
     int64_t M, N;
     const ModeGroup *mg, *ng;
     const int *eA, *eB; // exponents of rows / columns of this (item, batch)
@@ -96,6 +98,8 @@ __device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *
     TileJob j;
     if (!GROUPED) {
         int b;
+        const int ks = t % p.ksplit;
+        t /= p.ksplit;
         if (CL == 1) {
             tile_coords(p, t, b, j.mt, j.nt);
         } else {
@@ -107,7 +111,9 @@ __device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *
         }
         j.zA = b * p.S;
         j.zB = b * p.S;
-        j.nkb = p.nkb;
+        j.kbeg = ks * p.kslice;
+        j.nkb = min(p.kslice, p.nkb - j.kbeg);
+        j.tid = (b * p.mtiles + j.mt) * p.ntiles + j.nt;
         j.M = p.M;
         j.N = p.N;
         j.mg = &p.mg;
@@ -125,7 +131,9 @@ __device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *
         j.nt = w.w;
         j.zA = it.zA + b * p.S;
         j.zB = it.zB + b * p.S;
+        j.kbeg = 0;
         j.nkb = it.nkb;
+        j.tid = 0;
         j.M = it.M;
         j.N = it.N;
         j.mg = &it.mg;
@@ -137,6 +145,14 @@ __device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *
         j.C = it.C + oc;
     }
     return j;
+}
+
+// K blocks of schedule entry t.
+template <bool GROUPED>
+__device__ __forceinline__ int entry_nkb(const TcGemmParams &p, const TcItem *items, const int4 *work, int t) {
+    if (GROUPED) return items[work[t].x].nkb;
+    const int kbeg = (t % p.ksplit) * p.kslice;
+    return min(p.kslice, p.nkb - kbeg);
 }
 
 __device__ __forceinline__ double scale_pow2(double v, int e) {
@@ -281,7 +297,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint32_t crank = CL > 1 ? ptx::cluster_ctarank() : 0u;
     const int cta0 = blockIdx.x / CL, ctas = gridDim.x / CL; // schedule index and stride of this cluster
 
-    const int total_tiles = GROUPED ? ntiles_total : p.nbatch * (p.mtiles / CL) * p.ntiles;
+    const int total_tiles = GROUPED ? ntiles_total : p.nbatch * (p.mtiles / CL) * p.ntiles * p.ksplit;
     const int S = p.S;
 
     if (warp == 0) {
@@ -311,7 +327,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             uint8_t *sa = smem + stage * STAGE_BYTES;
 #pragma unroll
                             for (int h = 0; h < GROUP_KB; h++) {
-                                const int kc = (p.kb0 + kb + h) * kBK;
+                                const int kc = (p.kb0 + job.kbeg + kb + h) * kBK;
                                 ptx::tma_load_3d(sa + h * A_BYTES, &tmA, &full[stage], kc, job.mt * kBM, job.zA + s);
                                 uint8_t *sb = sa + GROUP_KB * A_BYTES + h * B_BYTES;
                                 if (CL == 1) {
@@ -358,7 +374,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             // Position in the group sequence: tile, slice group d, pair s, group g
             // of the pair (gpp groups per pair), groups in the open chunk.
             int tile = cta0, d = 0, s = 0, g = 0, in_chunk = 0;
-            int gpp = tile < total_tiles ? (GROUPED ? items[work[tile].x].nkb : p.nkb) / GROUP_KB : 0;
+            int gpp = tile < total_tiles ? entry_nkb<GROUPED>(p, items, work, tile) / GROUP_KB : 0;
             auto close_chunk = [&]() {
                 ptx::mma_commit(&accf[abuf]);
                 abuf ^= 1;
@@ -408,7 +424,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             d = 0;
                             tile += ctas;
                             if (tile >= total_tiles) return false;
-                            gpp = (GROUPED ? items[work[tile].x].nkb : p.nkb) / GROUP_KB;
+                            gpp = entry_nkb<GROUPED>(p, items, work, tile) / GROUP_KB;
                         }
                     }
                 }
@@ -452,6 +468,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         long long *const rbc = p.rbuf + (size_t)blockIdx.x * kBM * kBN;
         bool pend = false, pend_row_ok = false;
         bool pend_rows_fast = false; // C is contiguous along the rows: one thread per row stays coalesced
+        const long long *pend_src = rbc; // the pending tile's sums (scratch, or the K slices' accumulator)
         int pend_done = 0, pend_rowExp = 0;
         double *pend_C = nullptr;
         auto finalize_cols = [&](int upto) {
@@ -462,7 +479,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         long long Rv[kFinCols];
                         double old[kFinCols];
 #pragma unroll
-                        for (int i = 0; i < kFinCols; i++) Rv[i] = rbc[(size_t)(col0 + c0 + i) * kBM + row];
+                        for (int i = 0; i < kFinCols; i++) Rv[i] = __ldcg(pend_src + (size_t)(col0 + c0 + i) * kBM + row);
                         if (!plain_store) {
 #pragma unroll
                             for (int i = 0; i < kFinCols; i++)
@@ -492,7 +509,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         const int ce = colExp[c0 + i];
                         double v = 0.0;
                         if (pend_row_ok && ce != INT_MAX) {
-                            long long R = rbc[(size_t)(col0 + c0 + i) * kBM + row];
+                            long long R = __ldcg(pend_src + (size_t)(col0 + c0 + i) * kBM + row);
                             if (p.ab_neg) R = -R;
                             if (pend_rowExp == INT_MIN || ce == INT_MIN)
                                 v = __longlong_as_double(0x7ff8000000000000ll);
@@ -529,7 +546,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         for (int tile = cta0; tile < total_tiles && ok; tile += ctas) {
             // Only the K block count is held through the chunks; the rest of the
             // tile's description is resolved at its end (registers are scarce here).
-            const int nkb = GROUPED ? items[work[tile].x].nkb : p.nkb;
+            const int nkb = entry_nkb<GROUPED>(p, items, work, tile);
             // Running sum of this thread's 64 outputs, R = H + L: L (int32, registers)
             // takes every chunk, H (int64, TMEM columns 256..511) is written only when
             // L is folded in -- at the end of each slice group (Horner step R *= 256)
@@ -620,6 +637,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                 group_offsets32(*job.mg, (uint32_t)m, oa, ob, rowOff);
                 rowExp = job.eA[m];
             }
+            // K slices add their sums into the tile's accumulator; only the last
+            // one to arrive at this warp's region finishes it
+            long long *const dst = p.ksplit > 1 ? p.racc + (size_t)job.tid * kBM * kBN : rbc;
 #pragma unroll 1
             for (int cc = 0; cc < kBN / 32; cc++) {
                 const uint32_t col = (uint32_t)(col0 + cc * 16);
@@ -628,10 +648,25 @@ __global__ void __launch_bounds__(THREADS, 1)
                 ptx::tmem_ld16(tl + 384u + col, hi);
                 ptx::tmem_wait_ld();
 #pragma unroll
-                for (int i = 0; i < 16; i++)
-                    rbc[(size_t)(col0 + cc * 16 + i) * kBM + row] = (long long)(((unsigned long long)hi[i] << 32) | lo[i]);
+                for (int i = 0; i < 16; i++) {
+                    const unsigned long long R = ((unsigned long long)hi[i] << 32) | lo[i];
+                    long long *q = dst + (size_t)(col0 + cc * 16 + i) * kBM + row;
+                    if (p.ksplit > 1)
+                        atomicAdd((unsigned long long *)q, R); // two's complement: exact for signed sums
+                    else
+                        *q = (long long)R;
+                }
             }
             ptx::tc_fence_before();
+            bool finish = true;
+            if (p.ksplit > 1) {
+                __threadfence();
+                __syncwarp();
+                int last = 0;
+                if (lane == 0) last = atomicAdd(p.rcnt + job.tid * 8 + ew, 1) == p.ksplit - 1;
+                finish = __shfl_sync(0xffffffffu, last, 0) != 0;
+                if (finish) __threadfence();
+            }
             for (int i = lane; i < kBN / 2; i += 32) {
                 const int64_t n = (int64_t)job.nt * kBN + col0 + i;
                 int64_t oa, ob, oc = 0;
@@ -647,7 +682,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             rowOffW[lane] = rowOff;
             rowOkW[lane] = row_ok ? 1 : 0;
             __syncwarp();
-            pend = true;
+            pend = finish;
+            pend_src = dst;
             pend_done = 0;
             pend_row_ok = row_ok;
             pend_rows_fast = job.mg->n > 0 && job.mg->s[2][job.mg->n - 1] == 1;
@@ -690,7 +726,7 @@ eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const C
                          const TcGemmParams &p, cudaStream_t s) {
     eg_status st = ensure_tc_attributes();
     if (st != EG_SUCCESS) return st;
-    const int total = p.nbatch * p.mtiles * p.ntiles;
+    const int total = p.nbatch * p.mtiles * p.ntiles * p.ksplit;
     if (total <= 0) return EG_SUCCESS;
     if (p.mtiles % 2 == 0) {
         // clusters of two CTAs on vertically adjacent tiles share B through multicast

@@ -114,6 +114,24 @@ def test_gemv_shapes_run_fp64(eg):
     assert rep["slices"] == 5 and err < TOL_SPLIT, err
 
 
+def test_k_slices_in_parallel(eg):
+    # few output tiles and a long K: the K range runs in slices on different CTAs whose
+    # exact int64 sums are added atomically; the result is exact-order independent
+    err, rep = run_case(eg, "ij", "ik", "kj", {"i": 130, "j": 120, "k": 8192}, cp=0.7, ab=-0.3)
+    assert rep["slices"] == 5 and err < TOL_SPLIT, err
+    rng = np.random.default_rng(21)
+    A, B = cu(rng.standard_normal((200, 6000))), cu(rng.standard_normal((6000, 140)))
+    C0 = cu(rng.standard_normal((200, 140)))
+    outs = []
+    for _ in range(3):
+        C = C0.clone()
+        eg.einsum(0.5, "ij", C, 1.5, "ik", A, "kj", B, precision="split_bf16")
+        outs.append(C.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    ref = 0.5 * C0.cpu().numpy() + 1.5 * (A.cpu().numpy() @ B.cpu().numpy())
+    assert oracle.rel_fro(outs[0], ref) < TOL_SPLIT
+
+
 def test_rows_with_wide_dynamic_range(eg):
     err, _ = run_case(eg, "ij", "ik", "kj", {"i": 150, "j": 140, "k": 300}, scale_rows=True)
     assert err < TOL_SPLIT, err
