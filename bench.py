@@ -333,8 +333,10 @@ def run_ours(args, rank, world):
         avg_ms = d["total_ms"] / d["launches"]
         if headline == "split_bf16":
             pairs = (split_report or {}).get("slice_pairs", 0)
-            # bf16 flops issued by the tensor kernel per step (slice pairs x 2MNK over the GEMM-shaped W's)
-            alg = pairs * (F["Wmnij"] + F["Wabef"] + F["Wmbej"]) / (d["launches"] / args.steps)
+            # bf16 flops issued by the tensor kernel per launch (slice pairs x 2MNK over the GEMM-shaped W's);
+            # the kernel profile spans the warm-up and the timed steps
+            launches_per_step = d["launches"] / (args.steps + args.warmup)
+            alg = pairs * (F["Wmnij"] + F["Wabef"] + F["Wmbej"]) / launches_per_step
             ach = alg / (avg_ms * 1e-3) / 1e12
             peak = pk.get("bf16_tflops_sustained", 1700.0)
             roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
@@ -381,7 +383,7 @@ def run_ours(args, rank, world):
             "plain_fp64": {"value": fp64_value, "ms_per_step": ms_fp64, "per_contraction_ms": per_contraction_fp64,
                            "fp64_peak_tflops": fp64_peak, "dfma_tflops": dfma.value, "dmma_tflops": dmma.value},
             "split_vs_fp64_speedup": value / world / fp64_value if headline == "split_bf16" else None,
-            "per_contraction_ms": per_contraction, "kernels": kernels,
+            "per_contraction_ms": per_contraction, "kernels": kernels, "kernels_steps": args.steps + args.warmup,
             "error_vs_fp64": errors, "error_fp64_vs_oracle_sample": oracle_err, "split_report": split_report,
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches,
         }
