@@ -153,50 +153,64 @@ __global__ void k_split_exponent(const unsigned long long *rowmax, int *e, int64
     }
 }
 
-// 32x32 tiles staged through shared memory so that the operand is read along its
-// contiguous mode and the digit planes are written along k; padding rows and
-// columns are written as 0.
+// Tiles of 32 rows x 64 k staged through shared memory so that the operand is
+// read along its contiguous mode; each thread then converts two consecutive k
+// of a row and writes them as one BF16 pair per digit plane (a warp stores 128
+// contiguous bytes per plane).  Padding rows and columns are written as 0.
+constexpr int TK = 2 * T;
+template <int S>
 __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const double *__restrict__ X, const int *rexp,
-                                                        __nv_bfloat16 *planes, int S, int row_fast) {
-    __shared__ double tile[T][T + 1];
+                                                        __nv_bfloat16 *planes, int row_fast) {
+    __shared__ double tile[T][TK + 1];
     __shared__ int ex[T];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int64_t rt = m.Rp / T, kt = m.Kp / T;
+    const int64_t rt = m.Rp / T, kt = m.Kp / TK;
     const int64_t work = (int64_t)m.nbatch * rt * kt;
     const int64_t plane = m.Rp * m.Kp;
     for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
         const int64_t ktile = w % kt, rtile = (w / kt) % rt, b = w / (kt * rt);
         const int64_t ob = off_b(m, b);
-        const int64_t r0 = rtile * T, k0 = ktile * T;
+        const int64_t r0 = rtile * T, k0 = ktile * TK;
         if (ty == 0) ex[tx] = (r0 + tx < m.rows) ? rexp[b * m.Rp + r0 + tx] : 0;
         if (row_fast) {
             const int64_t r = r0 + tx;
-            const int64_t orow = r < m.rows ? ob + off_r(m, r) : 0;
-            for (int j = ty; j < T; j += TR) {
+            const double *xr = r < m.rows ? X + ob + off_r(m, r) : nullptr;
+#pragma unroll
+            for (int j = ty; j < TK; j += TR) {
                 const int64_t k = k0 + j;
-                tile[tx][j] = (r < m.rows && k < m.K) ? __ldg(X + orow + off_k(m, k)) : 0.0;
+                tile[tx][j] = (xr && k < m.K) ? __ldg(xr + off_k(m, k)) : 0.0;
             }
         } else {
-            const int64_t k = k0 + tx;
-            const int64_t okk = k < m.K ? off_k(m, k) : 0;
-            for (int j = ty; j < T; j += TR) {
-                const int64_t r = r0 + j;
-                tile[j][tx] = (r < m.rows && k < m.K) ? __ldg(X + ob + off_r(m, r) + okk) : 0.0;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int64_t k = k0 + h * T + tx;
+                const bool kin = k < m.K;
+                const int64_t okk = kin ? off_k(m, k) : 0;
+#pragma unroll
+                for (int j = ty; j < T; j += TR) {
+                    const int64_t r = r0 + j;
+                    tile[j][h * T + tx] = (r < m.rows && kin) ? __ldg(X + ob + off_r(m, r) + okk) : 0.0;
+                }
             }
         }
         __syncthreads();
-        // write: consecutive threads walk k in every digit plane
+        // write: thread tx converts k0 + 2tx and k0 + 2tx + 1 of each of its rows
+#pragma unroll
         for (int j = ty; j < T; j += TR) {
             const int64_t r = r0 + j;
-            int dig[kMaxSlices];
+            int d0[S], d1[S];
             const int e = ex[j];
             if (e == INT_MIN) {
-                for (int s = 0; s < S; s++) dig[s] = 0;
+#pragma unroll
+                for (int s = 0; s < S; s++) d0[s] = d1[s] = 0;
             } else {
-                to_digits(tile[j][tx], e, S, dig);
+                to_digits(tile[j][2 * tx], e, S, d0);
+                to_digits(tile[j][2 * tx + 1], e, S, d1);
             }
-            __nv_bfloat16 *out = planes + ((int64_t)b * S) * plane + r * m.Kp + k0 + tx;
-            for (int s = 0; s < S; s++) out[(int64_t)s * plane] = __float2bfloat16_rn((float)dig[s]);
+            __nv_bfloat162 *out = (__nv_bfloat162 *)(planes + ((int64_t)b * S) * plane + r * m.Kp + k0) + tx;
+#pragma unroll
+            for (int s = 0; s < S; s++)
+                out[(int64_t)s * (plane / 2)] = __floats2bfloat162_rn((float)d0[s], (float)d1[s]);
         }
         __syncthreads();
     }
@@ -276,10 +290,17 @@ eg_status split_operand(OperandMap om, const double *X, unsigned long long *rowm
     }
     EG_CHECK_LAUNCH("k_split_exponent");
     {
-        const int64_t work = (int64_t)om.nbatch * (om.Rp / T) * (om.Kp / T);
+        const int64_t work = (int64_t)om.nbatch * (om.Rp / T) * (om.Kp / TK);
         const int grid = (int)(work < 2 * cap ? work : 2 * cap);
         LaunchScope ls_("k_split_digits", s);
-        k_split_digits<<<grid, dim3(T, TR), 0, s>>>(om, X, rexp, planes, S, r_fast ? 1 : 0);
+        const int rf = r_fast ? 1 : 0;
+        switch (S) {
+        case 2: k_split_digits<2><<<grid, dim3(T, TR), 0, s>>>(om, X, rexp, planes, rf); break;
+        case 3: k_split_digits<3><<<grid, dim3(T, TR), 0, s>>>(om, X, rexp, planes, rf); break;
+        case 4: k_split_digits<4><<<grid, dim3(T, TR), 0, s>>>(om, X, rexp, planes, rf); break;
+        case 5: k_split_digits<5><<<grid, dim3(T, TR), 0, s>>>(om, X, rexp, planes, rf); break;
+        default: k_split_digits<6><<<grid, dim3(T, TR), 0, s>>>(om, X, rexp, planes, rf); break;
+        }
     }
     EG_CHECK_LAUNCH("k_split_digits");
     return EG_SUCCESS;

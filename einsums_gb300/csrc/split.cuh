@@ -111,6 +111,7 @@ __device__ __forceinline__ long long scaled_round(double x, int sh) {
 // most significant first: dig[0] in [-128, 128], the others in [-127, 128].
 __device__ __forceinline__ void to_digits(double x, int e, int S, int *dig) {
     long long F = scaled_round(x, kTopBits + kBits * (S - 1) - e);
+#pragma unroll
     for (int s = S - 1; s >= 1; s--) {
         int d = (int)(F & 255);
         if (d > 128) d -= 256;
