@@ -13,6 +13,9 @@
 //   k_contract_f64  general case: 64x64 register-tiled DFMA contraction
 //                   (replaces hipblasDgemm_64 and the atomicAdd generic kernel
 //                    GPUTensorAlgebra.hpp:28-82)
+#include <algorithm>
+#include <utility>
+
 #include "common.cuh"
 
 namespace eg {
@@ -135,34 +138,65 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_final(const double *partial
 // ------------------------------------------------------------------- gemv --
 // Output positions are walked through `rows` (batch and the non-empty M or N
 // group, offsets in A/B/C); every output sums over `k`.
+// KContig: k is one mode of stride 1 in A and B.  Otherwise the offsets of
+// every k in A and B come from tables (offk[0..K) for A, offk[K..2K) for B),
+// or, when offk is null, from the mode decomposition.  Four independent
+// accumulators keep four loads of each operand in flight per thread.
 template <int TPR, bool KContig>
 __global__ void __launch_bounds__(256) k_gemv(ModeGroup rows, ModeGroup k, const double *__restrict__ A,
                                               const double *__restrict__ B, double *C, double cp, double ab,
-                                              bool zero) {
+                                              bool zero, const int64_t *__restrict__ offk) {
     __shared__ double smem[32];
     constexpr int RPB = 256 / TPR; // rows per block
     const int sub = threadIdx.x / TPR, lane = threadIdx.x % TPR;
+    const int64_t K = k.total;
     for (int64_t r = (int64_t)blockIdx.x * RPB + sub; r < rows.total; r += (int64_t)gridDim.x * RPB) {
         int64_t ra, rb, rc;
         group_offsets(rows, r, ra, rb, rc);
         const double *a = A + ra;
         const double *b = B + rb;
-        double acc0 = 0.0, acc1 = 0.0;
-        if (KContig) {
-            int64_t i = lane;
-            for (; i + TPR < k.total; i += 2 * TPR) {
-                acc0 = fma(__ldg(a + i), __ldg(b + i), acc0);
-                acc1 = fma(__ldg(a + i + TPR), __ldg(b + i + TPR), acc1);
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        int64_t i = lane;
+        if (KContig && ((((uintptr_t)a) | ((uintptr_t)b)) & 15) == 0) {
+            // 16-byte pairs: eight values of each operand in flight per thread
+            const double2 *a2 = (const double2 *)a, *b2 = (const double2 *)b;
+            const int64_t K2 = K / 2;
+            int64_t j = lane;
+            for (; j + 3 * TPR < K2; j += 4 * TPR) {
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const double2 x = __ldg(a2 + j + u * TPR), y = __ldg(b2 + j + u * TPR);
+                    acc[u] = fma(x.x, y.x, acc[u]);
+                    acc[u] = fma(x.y, y.y, acc[u]);
+                }
             }
-            if (i < k.total) acc0 = fma(__ldg(a + i), __ldg(b + i), acc0);
+            for (; j < K2; j += TPR) {
+                const double2 x = __ldg(a2 + j), y = __ldg(b2 + j);
+                acc[0] = fma(x.x, y.x, acc[0]);
+                acc[0] = fma(x.y, y.y, acc[0]);
+            }
+            if ((K & 1) && lane == 0) acc[1] = fma(__ldg(a + K - 1), __ldg(b + K - 1), acc[1]);
+        } else if (KContig) {
+            for (; i + 3 * TPR < K; i += 4 * TPR) {
+#pragma unroll
+                for (int u = 0; u < 4; u++) acc[u] = fma(__ldg(a + i + u * TPR), __ldg(b + i + u * TPR), acc[u]);
+            }
+            for (; i < K; i += TPR) acc[0] = fma(__ldg(a + i), __ldg(b + i), acc[0]);
+        } else if (offk) {
+            for (; i + 3 * TPR < K; i += 4 * TPR) {
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+                    acc[u] = fma(__ldg(a + __ldg(offk + i + u * TPR)), __ldg(b + __ldg(offk + K + i + u * TPR)), acc[u]);
+            }
+            for (; i < K; i += TPR) acc[0] = fma(__ldg(a + __ldg(offk + i)), __ldg(b + __ldg(offk + K + i)), acc[0]);
         } else {
-            for (int64_t i = lane; i < k.total; i += TPR) {
+            for (; i < K; i += TPR) {
                 int64_t oa, ob, oc;
                 group_offsets32(k, (uint32_t)i, oa, ob, oc);
-                acc0 = fma(__ldg(a + oa), __ldg(b + ob), acc0);
+                acc[0] = fma(__ldg(a + oa), __ldg(b + ob), acc[0]);
             }
         }
-        double s = acc0 + acc1;
+        double s = (acc[0] + acc[1]) + (acc[2] + acc[3]);
         if (TPR == 32) {
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         } else {
@@ -170,6 +204,101 @@ __global__ void __launch_bounds__(256) k_gemv(ModeGroup rows, ModeGroup k, const
         }
         if (lane == 0) C[rc] = epilogue(s, C + rc, cp, ab, zero);
         if (TPR != 32) __syncthreads();
+    }
+}
+
+// Long k: one CTA takes RB outputs at a time, each k of B (the vector, shared
+// by every output) and each pair of table offsets is loaded once and used for
+// RB rows of A, so the vector's L1 traffic and the reductions are divided by
+// RB.  Contig: k is one mode of stride 1 in A and B (with 16-byte pairs when
+// aligned); otherwise offk[0..K) / offk[K..2K) hold the offsets of every k in A
+// and B.
+template <int RB, bool Contig>
+__global__ void __launch_bounds__(256) k_gemv_rows(ModeGroup rows, ModeGroup k, const double *__restrict__ A,
+                                                   const double *__restrict__ B, double *C, double cp, double ab,
+                                                   bool zero, const int64_t *__restrict__ offk) {
+    __shared__ double red[8][RB];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t K = k.total;
+    for (int64_t r0 = (int64_t)blockIdx.x * RB; r0 < rows.total; r0 += (int64_t)gridDim.x * RB) {
+        const double *a[RB];
+        const double *b = B;
+        bool aligned = true;
+#pragma unroll
+        for (int q = 0; q < RB; q++) {
+            const int64_t r = r0 + q < rows.total ? r0 + q : rows.total - 1; // tail rows repeat the last one
+            int64_t ra, rb, oc;
+            group_offsets(rows, r, ra, rb, oc);
+            a[q] = A + ra;
+            b = B + rb; // the same for every row: the rows run over A's modes only
+            aligned &= (((uintptr_t)a[q]) & 15) == 0;
+        }
+        aligned &= (((uintptr_t)b) & 15) == 0;
+        double acc[RB];
+#pragma unroll
+        for (int q = 0; q < RB; q++) acc[q] = 0.0;
+        if (Contig && aligned) {
+            const int64_t K2 = K / 2;
+            // CTAs start at different points of k so that concurrently read rows
+            // (a fixed stride apart) do not hit the same memory channels in step
+            const int64_t start = K2 > 4096 ? ((r0 / RB) * 1031 % (K2 / 256)) * 256 : 0;
+            auto body = [&](int64_t j) {
+                const double2 y = __ldg((const double2 *)b + j);
+#pragma unroll
+                for (int q = 0; q < RB; q++) {
+                    const double2 x = __ldg((const double2 *)a[q] + j);
+                    acc[q] = fma(x.x, y.x, acc[q]);
+                    acc[q] = fma(x.y, y.y, acc[q]);
+                }
+            };
+            for (int64_t j = start + tid; j < K2; j += 256) body(j);
+            for (int64_t j = tid; j < start; j += 256) body(j);
+            if ((K & 1) && tid == 0) {
+                const double y = __ldg(b + K - 1);
+#pragma unroll
+                for (int q = 0; q < RB; q++) acc[q] = fma(__ldg(a[q] + K - 1), y, acc[q]);
+            }
+        } else if (Contig) {
+            for (int64_t i = tid; i < K; i += 256) {
+                const double y = __ldg(b + i);
+#pragma unroll
+                for (int q = 0; q < RB; q++) acc[q] = fma(__ldg(a[q] + i), y, acc[q]);
+            }
+        } else {
+            for (int64_t i = tid; i < K; i += 256) {
+                const int64_t oa = __ldg(offk + i);
+                const double y = __ldg(b + __ldg(offk + K + i));
+#pragma unroll
+                for (int q = 0; q < RB; q++) acc[q] = fma(__ldg(a[q] + oa), y, acc[q]);
+            }
+        }
+        // fixed-order reduction: warp trees, then the warps in order
+#pragma unroll
+        for (int q = 0; q < RB; q++) {
+            double v = acc[q];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[warp][q] = v;
+        }
+        __syncthreads();
+        if (tid < RB && r0 + tid < rows.total) {
+            double v = 0.0;
+            for (int w = 0; w < 8; w++) v += red[w][tid];
+            int64_t ra, rb, oc;
+            group_offsets(rows, r0 + tid, ra, rb, oc);
+            C[oc] = epilogue(v, C + oc, cp, ab, zero);
+        }
+        __syncthreads();
+    }
+}
+
+// Offsets of every k of a mode group in A (out[0..K)) and in B (out[K..2K)).
+__global__ void k_k_offsets(ModeGroup k, int64_t *out) {
+    const int64_t K = k.total;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < K; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t oa, ob, oc;
+        group_offsets32(k, (uint32_t)i, oa, ob, oc);
+        out[i] = oa;
+        out[K + i] = ob;
     }
 }
 
@@ -356,29 +485,55 @@ eg_status launch_dot(const Contraction &c, cudaStream_t s) {
 
 eg_status launch_gemv(const Contraction &c, cudaStream_t s) {
     ModeGroup rows = concat({&c.batch, &c.m, &c.n});
-    const ModeGroup &k = c.k;
+    ModeGroup k = c.k;
     if (!fits32(k)) return fail(EG_ERROR_NOT_SUPPORTED, "gemv: summed extent exceeds 2^31");
     const bool contig = k.n == 1 && k.s[0][0] == 1 && k.s[1][0] == 1;
-    if (k.total >= 2048) {
-        const int grid = grid_for(rows.total, 1);
+    // Long k, unbatched, one free group: the operand without free modes is a
+    // vector shared by every output, and k_gemv_rows reuses it for RB rows.  It
+    // takes the rows from its first operand, so when they run over B's modes
+    // (M empty) the operands and their stride components are swapped.
+    const bool rows_kernel = k.total >= 2048 && c.batch.n == 0 && (c.m.n == 0) != (c.n.n == 0);
+    const double *X = c.A, *Y = c.B;
+    if (rows_kernel && c.m.n == 0) {
+        for (int d = 0; d < rows.n; d++) std::swap(rows.s[0][d], rows.s[1][d]);
+        for (int d = 0; d < k.n; d++) std::swap(k.s[0][d], k.s[1][d]);
+        std::swap(X, Y);
+    }
+    // offset tables for a strided k, built once and shared by every output
+    int64_t *offk = nullptr;
+    if (!contig && k.total <= (int64_t(1) << 24) && rows.total > 1) {
+        void *ws = nullptr;
+        eg_status st = workspace(s, (size_t)k.total * 2 * sizeof(int64_t), &ws);
+        if (st != EG_SUCCESS) return st;
+        offk = (int64_t *)ws;
+        {
+            LaunchScope ls_("k_k_offsets", s);
+            k_k_offsets<<<(int)std::min<int64_t>((k.total + 255) / 256, (int64_t)num_sms() * 8), 256, 0, s>>>(k, offk);
+        }
+        EG_CHECK_LAUNCH("k_k_offsets");
+    }
+    if (rows_kernel && (contig || offk)) {
+        constexpr int RB = 4;
+        const int grid = grid_for(rows.total, RB);
+        LaunchScope ls_("k_gemv", s);
         if (contig)
-            { LaunchScope ls_("k_gemv", s);
-            k_gemv<256, true><<<grid, 256, 0, s>>>(rows, k, c.A, c.B, c.C, c.cp, c.ab, c.zero_when_cp_zero);
-            }
+            k_gemv_rows<RB, true><<<grid, 256, 0, s>>>(rows, k, X, Y, c.C, c.cp, c.ab, c.zero_when_cp_zero, nullptr);
         else
-            { LaunchScope ls_("k_gemv", s);
-            k_gemv<256, false><<<grid, 256, 0, s>>>(rows, k, c.A, c.B, c.C, c.cp, c.ab, c.zero_when_cp_zero);
-            }
+            k_gemv_rows<RB, false><<<grid, 256, 0, s>>>(rows, k, X, Y, c.C, c.cp, c.ab, c.zero_when_cp_zero, offk);
+    } else if (k.total >= 2048) {
+        const int grid = grid_for(rows.total, 1);
+        LaunchScope ls_("k_gemv", s);
+        if (contig)
+            k_gemv<256, true><<<grid, 256, 0, s>>>(rows, k, X, Y, c.C, c.cp, c.ab, c.zero_when_cp_zero, nullptr);
+        else
+            k_gemv<256, false><<<grid, 256, 0, s>>>(rows, k, X, Y, c.C, c.cp, c.ab, c.zero_when_cp_zero, offk);
     } else {
         const int grid = grid_for(rows.total, 8);
+        LaunchScope ls_("k_gemv", s);
         if (contig)
-            { LaunchScope ls_("k_gemv", s);
-            k_gemv<32, true><<<grid, 256, 0, s>>>(rows, k, c.A, c.B, c.C, c.cp, c.ab, c.zero_when_cp_zero);
-            }
+            k_gemv<32, true><<<grid, 256, 0, s>>>(rows, k, X, Y, c.C, c.cp, c.ab, c.zero_when_cp_zero, nullptr);
         else
-            { LaunchScope ls_("k_gemv", s);
-            k_gemv<32, false><<<grid, 256, 0, s>>>(rows, k, c.A, c.B, c.C, c.cp, c.ab, c.zero_when_cp_zero);
-            }
+            k_gemv<32, false><<<grid, 256, 0, s>>>(rows, k, X, Y, c.C, c.cp, c.ab, c.zero_when_cp_zero, offk);
     }
     EG_CHECK_LAUNCH("k_gemv");
     return EG_SUCCESS;

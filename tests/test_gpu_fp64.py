@@ -252,3 +252,38 @@ def test_empty_and_degenerate(eg):
     C = z(3, 3).fill_(2.0)
     eg.einsum(0.5, "ij", C, 1.0, "ik", z(3, 0), "kj", z(0, 3))
     assert torch.all(C == 1.0)
+
+
+@pytest.mark.parametrize("case", ["rows_contig_odd", "rows_misaligned", "vector_times_matrix", "strided_k",
+                                  "strided_k_rows_over_B", "tail_rows"])
+def test_long_k_gemv_variants(eg, case):
+    # long k (>= 2048) GEMV shapes: the multi-row kernel, contiguous (16-byte pairs or not),
+    # strided through offset tables, and with the operands swapped when the rows run over B
+    rng = np.random.default_rng(abs(hash(case)) % 1000)
+    if case == "rows_contig_odd":
+        Cl, Al, Bl, A, B = "p", "pk", "k", rng.standard_normal((103, 3001)), rng.standard_normal(3001)
+    elif case == "rows_misaligned":
+        A_np, B_np = rng.standard_normal((40, 2501)), rng.standard_normal(2501)
+        tA, tB = cu(A_np)[:, 1:], cu(B_np)[1:]  # 8-byte offsets: no 16-byte pairs
+        ref = A_np[:, 1:] @ B_np[1:]
+        C = torch.zeros(40, dtype=torch.float64, device="cuda")
+        eg.einsum(0.0, "p", C, 1.0, "pk", tA, "k", tB)
+        assert oracle.rel_fro(C.cpu().numpy(), ref) < TOL
+        return
+    elif case == "vector_times_matrix":
+        Cl, Al, Bl, A, B = "q", "k", "kq", rng.standard_normal(2600), rng.standard_normal((2600, 77))
+    elif case == "strided_k":
+        Cl, Al, Bl, A, B = "pq", "prqs", "rs", rng.standard_normal((9, 60, 9, 50)), rng.standard_normal((60, 50))
+    elif case == "strided_k_rows_over_B":
+        Cl, Al, Bl, A, B = "pq", "rs", "prqs", rng.standard_normal((60, 50)), rng.standard_normal((9, 60, 9, 50))
+    else:  # rows not a multiple of the rows per block
+        Cl, Al, Bl, A, B = "p", "pk", "k", rng.standard_normal((7, 4096)), rng.standard_normal(4096)
+    dims = {}
+    for l, e in list(zip(Al, A.shape)) + list(zip(Bl, B.shape)):
+        dims[l] = e
+    C0 = rng.standard_normal([dims[l] for l in Cl])
+    ref = C0.copy()
+    oracle.einsum(Cl, ref, 0.5, -1.5, Al, A, Bl, B)
+    tC = cu(C0)
+    eg.einsum(0.5, Cl, tC, -1.5, Al, cu(A), Bl, cu(B))
+    assert oracle.rel_fro(tC.cpu().numpy(), ref) < TOL
