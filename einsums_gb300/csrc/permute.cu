@@ -49,25 +49,43 @@ __device__ __forceinline__ double combine(double a, const double *c, double ap, 
     return __dadd_rn(__dmul_rn(ap, a), __dmul_rn(cp, *c));
 }
 
-// Fastest modes shared: rows of length L with strides sa/sc along the row.
+// Fastest modes shared: rows of length L with strides sa/sc along the row.  A
+// warp takes a chunk of up to kRowChunk elements of one row (the decomposition
+// of the row index is paid once per chunk) and keeps four loads in flight.
+constexpr int64_t kRowChunk = 2048;
 template <int MODE>
 __global__ void __launch_bounds__(256) k_permute_rows(PermuteMap rest, int64_t L, int64_t sa, int64_t sc,
                                                       const double *__restrict__ A, double *C, double ap, double cp) {
-    const int64_t chunks = (L + 255) / 256;
-    const int64_t work = rest.total * chunks;
-    for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
-        const int64_t row = w / chunks, ch = w - row * chunks;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t chunks = (L + kRowChunk - 1) / kRowChunk;
+    const int64_t units = rest.total * chunks;
+    for (int64_t u = (int64_t)blockIdx.x * 8 + warp; u < units; u += (int64_t)gridDim.x * 8) {
+        const int64_t row = u / chunks, ch = u - row * chunks;
         int64_t oa, oc;
         rest_offsets(rest, row, oa, oc);
-        const int64_t x = ch * 256 + threadIdx.x;
-        if (x < L) {
-            double *cp_ = C + oc + x * sc;
-            *cp_ = combine<MODE>(__ldg(A + oa + x * sa), cp_, ap, cp);
+        const double *a = A + oa;
+        double *c = C + oc;
+        const int64_t x0 = ch * kRowChunk, x1 = min(L, x0 + kRowChunk);
+        int64_t x = x0 + lane;
+        for (; x + 96 < x1; x += 128) {
+            double v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) v[q] = __ldg(a + (x + 32 * q) * sa);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                double *cptr = c + (x + 32 * q) * sc;
+                *cptr = combine<MODE>(v[q], cptr, ap, cp);
+            }
+        }
+        for (; x < x1; x += 32) {
+            double *cptr = c + x * sc;
+            *cptr = combine<MODE>(__ldg(a + x * sa), cptr, ap, cp);
         }
     }
 }
 
 constexpr int TILE = 32, ROWS = 8;
+constexpr int64_t kStrip = 8; // tiles along C's fastest mode per work unit
 
 // ia runs along A's fastest mode (extent EA, strides saA in A / scA in C);
 // ic runs along C's fastest mode (extent EC, strides saC in A / scC in C).
@@ -79,33 +97,42 @@ __global__ void __launch_bounds__(TILE *ROWS) k_permute_tiles(PermuteMap rest, i
     __shared__ double tile[TILE][TILE + 1];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int64_t tilesA = (EA + TILE - 1) / TILE, tilesC = (EC + TILE - 1) / TILE;
-    const int64_t work = rest.total * tilesA * tilesC;
-    for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
-        int64_t t = w;
-        const int64_t tc = t % tilesC;
-        t /= tilesC;
-        const int64_t ta = t % tilesA;
-        const int64_t r = t / tilesA;
+    // a work unit is a strip: one index of the rest modes, one tile row along A's
+    // fastest mode and up to kStrip tiles along C's fastest mode, so that the
+    // decomposition of the unit is paid once per strip rather than per tile
+    const int64_t segs = (tilesC + kStrip - 1) / kStrip;
+    const int64_t units = rest.total * tilesA * segs;
+    for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
+        const int64_t sg = u % segs, ta = (u / segs) % tilesA, r = u / (segs * tilesA);
         int64_t oa, oc;
         rest_offsets(rest, r, oa, oc);
-        const int64_t a0 = ta * TILE, c0 = tc * TILE;
-        // read: consecutive threads walk A's fastest mode
+        const int64_t a0 = ta * TILE;
+        const double *Ar = A + oa + (a0 + tx) * saA;       // this thread's reads: ia = a0 + tx
+        const bool a_in = a0 + tx < EA;
+        const int64_t cbeg = sg * kStrip * TILE, cend = min(EC, cbeg + kStrip * TILE);
+        for (int64_t c0 = cbeg; c0 < cend; c0 += TILE) {
+            // read: consecutive threads walk A's fastest mode
 #pragma unroll
-        for (int j = 0; j < TILE; j += ROWS) {
-            const int64_t ia = a0 + tx, ic = c0 + ty + j;
-            if (ia < EA && ic < EC) tile[ty + j][tx] = __ldg(A + oa + ia * saA + ic * saC);
-        }
-        __syncthreads();
-        // write: consecutive threads walk C's fastest mode
-#pragma unroll
-        for (int j = 0; j < TILE; j += ROWS) {
-            const int64_t ic = c0 + tx, ia = a0 + ty + j;
-            if (ia < EA && ic < EC) {
-                double *cptr = C + oc + ia * scA + ic * scC;
-                *cptr = combine<MODE>(tile[tx][ty + j], cptr, ap, cp);
+            for (int j = 0; j < TILE; j += ROWS) {
+                const int64_t ic = c0 + ty + j;
+                if (a_in && ic < cend) tile[ty + j][tx] = __ldg(Ar + ic * saC);
             }
+            __syncthreads();
+            // write: consecutive threads walk C's fastest mode
+            const int64_t ic = c0 + tx;
+            if (ic < cend) {
+                double *Cc = C + oc + ic * scC;
+#pragma unroll
+                for (int j = 0; j < TILE; j += ROWS) {
+                    const int64_t ia = a0 + ty + j;
+                    if (ia < EA) {
+                        double *cptr = Cc + ia * scA;
+                        *cptr = combine<MODE>(tile[tx][ty + j], cptr, ap, cp);
+                    }
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
@@ -156,7 +183,7 @@ eg_status launch_permute(const PermuteDesc &p, cudaStream_t s) {
     }
     if (fa == fc) {
         const int64_t L = ext[fc];
-        const int64_t work = rest.total * ((L + 255) / 256);
+        const int64_t work = (rest.total * ((L + kRowChunk - 1) / kRowChunk) + 7) / 8;
         const int grid = (int)(work < cap ? work : cap);
         if (mode == 0)
             { LaunchScope ls_("k_permute_rows", s);
@@ -174,7 +201,7 @@ eg_status launch_permute(const PermuteDesc &p, cudaStream_t s) {
         return EG_SUCCESS;
     }
     const int64_t EA = ext[fa], EC = ext[fc];
-    const int64_t work = rest.total * ((EA + TILE - 1) / TILE) * ((EC + TILE - 1) / TILE);
+    const int64_t work = rest.total * ((EA + TILE - 1) / TILE) * (((EC + TILE - 1) / TILE + kStrip - 1) / kStrip);
     const int grid = (int)(work < cap ? work : cap);
     dim3 block(TILE, ROWS);
     if (mode == 0)
