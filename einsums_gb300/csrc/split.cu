@@ -158,27 +158,39 @@ __global__ void k_split_exponent(const unsigned long long *rowmax, int *e, int64
 // of a row and writes them as one BF16 pair per digit plane (a warp stores 128
 // contiguous bytes per plane).  Padding rows and columns are written as 0.
 constexpr int TK = 2 * T;
+constexpr int64_t kDigitStrip = 8; // k tiles per work unit
 template <int S>
 __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const double *__restrict__ X, const int *rexp,
                                                         __nv_bfloat16 *planes, int row_fast) {
     __shared__ double tile[T][TK + 1];
     __shared__ int ex[T];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int64_t rt = m.Rp / T, kt = m.Kp / TK;
-    const int64_t work = (int64_t)m.nbatch * rt * kt;
+    // a work unit is a strip of up to kDigitStrip k tiles of one 32-row tile, so
+    // that the unit's decomposition, exponents and row offsets are paid per strip
+    const int64_t rt = m.Rp / T, kt = m.Kp / TK, segs = (kt + kDigitStrip - 1) / kDigitStrip;
+    const int64_t work = (int64_t)m.nbatch * rt * segs;
     const int64_t plane = m.Rp * m.Kp;
+    constexpr int RPT = T / TR;
     for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
-        const int64_t ktile = w % kt, rtile = (w / kt) % rt, b = w / (kt * rt);
+        const int64_t sg = w % segs, rtile = (w / segs) % rt, b = w / (segs * rt);
         const int64_t ob = off_b(m, b);
-        const int64_t r0 = rtile * T, k0 = ktile * TK;
+        const int64_t r0 = rtile * T;
+        __syncthreads(); // the previous strip's last reads of ex[] are done
         if (ty == 0) ex[tx] = (r0 + tx < m.rows) ? rexp[b * m.Rp + r0 + tx] : 0;
+        const double *xr[RPT]; // row_fast: row r0+tx in xr[0]; else rows r0+ty+8j
+#pragma unroll
+        for (int j = 0; j < RPT; j++) {
+            const int64_t r = row_fast ? (j == 0 ? r0 + tx : m.rows) : r0 + ty + TR * j;
+            xr[j] = r < m.rows ? X + ob + off_r(m, r) : nullptr;
+        }
+        const int64_t kt_end = min(kt, (sg + 1) * kDigitStrip);
+        for (int64_t ktile = sg * kDigitStrip; ktile < kt_end; ktile++) {
+        const int64_t k0 = ktile * TK;
         if (row_fast) {
-            const int64_t r = r0 + tx;
-            const double *xr = r < m.rows ? X + ob + off_r(m, r) : nullptr;
 #pragma unroll
             for (int j = ty; j < TK; j += TR) {
                 const int64_t k = k0 + j;
-                tile[tx][j] = (xr && k < m.K) ? __ldg(xr + off_k(m, k)) : 0.0;
+                tile[tx][j] = (xr[0] && k < m.K) ? __ldg(xr[0] + off_k(m, k)) : 0.0;
             }
         } else {
 #pragma unroll
@@ -187,10 +199,7 @@ __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const doub
                 const bool kin = k < m.K;
                 const int64_t okk = kin ? off_k(m, k) : 0;
 #pragma unroll
-                for (int j = ty; j < T; j += TR) {
-                    const int64_t r = r0 + j;
-                    tile[j][h * T + tx] = (r < m.rows && kin) ? __ldg(X + ob + off_r(m, r) + okk) : 0.0;
-                }
+                for (int j = 0; j < RPT; j++) tile[ty + TR * j][h * T + tx] = (xr[j] && kin) ? __ldg(xr[j] + okk) : 0.0;
             }
         }
         __syncthreads();
@@ -213,6 +222,7 @@ __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const doub
                 out[(int64_t)s * (plane / 2)] = __floats2bfloat162_rn((float)d0[s], (float)d1[s]);
         }
         __syncthreads();
+        }
     }
 }
 
@@ -290,7 +300,7 @@ eg_status split_operand(OperandMap om, const double *X, unsigned long long *rowm
     }
     EG_CHECK_LAUNCH("k_split_exponent");
     {
-        const int64_t work = (int64_t)om.nbatch * (om.Rp / T) * (om.Kp / TK);
+        const int64_t work = (int64_t)om.nbatch * (om.Rp / T) * ((om.Kp / TK + kDigitStrip - 1) / kDigitStrip);
         const int grid = (int)(work < 2 * cap ? work : 2 * cap);
         LaunchScope ls_("k_split_digits", s);
         const int rf = r_fast ? 1 : 0;
