@@ -390,56 +390,87 @@ def run_ours(args, rank, world):
         print(json.dumps(line))
 
 
-def run_e2e(eg, T, precision, args, o, v, step_flops):
+def run_e2e(eg, T, precision, args, o, v, step_flops, chunks=8, return_outputs=False):
     """Same step through the public API with host buffers: every step copies all
     of its inputs in from pinned host memory and all four results back, inside
     the timed region.  The copies are pipelined the way a caller of the API
-    would: two device buffer sets; step i+1's inputs upload on one stream while
-    step i computes on another, and each W is read back on a third stream as soon
-    as its contraction is done.  A buffer set is refilled only after the reads of
-    its previous results have finished."""
+    would, on three streams (uploads, contractions, read-backs):
+
+    * t, g_oovv, g_oooo and g_ovvo (0.6 GB) go to one of three device sets;
+      Wmnij, Wmbej and E are computed from them and read back.
+    * Wabef's 5.2 GB initial value g_vvvv and its result move in ``chunks``
+      slabs of rows a: slab j uploads into one of four device slab buffers, its
+      contraction W[a0:a1] += 0.25 g_mnef t_mn[a0:a1]b runs as soon as it has
+      landed, and it is read back as soon as that is done.  Each output element
+      is computed exactly as in the whole contraction (its row and column and
+      the K sum are unchanged), so the slabs reproduce it bit for bit.
+
+    A set or slab buffer is refilled only after the read-back of its previous
+    contents has finished."""
     import torch
-    names = ("t", "g_oovv", "g_oooo", "g_ovvo", "g_vvvv")  # small inputs first, Wabef's 5 GB input last
-    host = {k: T[k].cpu().pin_memory() for k in names}
+    small = ("t", "g_oovv", "g_oooo", "g_ovvo")
+    host = {k: T[k].cpu().pin_memory() for k in small + ("g_vvvv",)}
     out = {"Wmnij": torch.empty_like(host["g_oooo"]).pin_memory(),
            "Wmbej": torch.empty_like(host["g_ovvo"]).pin_memory(),
            "Wabef": torch.empty_like(host["g_vvvv"]).pin_memory(),
            "E": torch.empty((), dtype=torch.float64).pin_memory()}
+    nv = host["g_vvvv"].shape[0]
+    chunks = max(1, min(chunks, nv))
+    bounds = [(nv * j // chunks, nv * (j + 1) // chunks) for j in range(chunks)]
+    rows_max = max(a1 - a0 for a0, a1 in bounds)
     sets = []
-    for _ in range(2):
-        dev = {k: torch.empty_like(T[k]) for k in names}
-        W = {"Wmnij": dev["g_oooo"], "Wabef": dev["g_vvvv"], "Wmbej": dev["g_ovvo"],
-             "E": torch.zeros((), dtype=torch.float64, device="cuda")}
-        sets.append((dev, W, torch.cuda.Event()))  # event: the set's results have been read back
+    for _ in range(3):
+        dev = {k: torch.empty_like(T[k]) for k in small}
+        W = {"Wmnij": dev["g_oooo"], "Wmbej": dev["g_ovvo"], "E": torch.zeros((), dtype=torch.float64, device="cuda")}
+        sets.append((dev, W, torch.cuda.Event()))  # event: the set's last use has finished
+    slabs = [(torch.empty((rows_max,) + tuple(host["g_vvvv"].shape[1:]), dtype=torch.float64, device="cuda"),
+              torch.cuda.Event()) for _ in range(4)]
     h2d = sum(x.numel() * 8 for x in host.values())
     d2h = sum(x.numel() * 8 for x in out.values())
     s_in, s_cmp, s_out = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
-    inputs_of = {"Wmnij": ("t", "g_oovv", "g_oooo"), "Wmbej": ("t", "g_oovv", "g_ovvo"),
-                 "Wabef": ("t", "g_oovv", "g_vvvv"), "E": ("t", "g_oovv")}
-    order = ("Wmnij", "Wmbej", "Wabef", "E")
+    inputs_of = {"Wmnij": ("t", "g_oovv", "g_oooo"), "Wmbej": ("t", "g_oovv", "g_ovvo"), "E": ("t", "g_oovv")}
+    counter = [0]
 
     def step(i):
-        dev, W, freed = sets[i % 2]
-        landed = {}
+        dev, W, freed = sets[i % 3]
+        landed, done = {}, {}
         s_in.wait_event(freed)
         with torch.cuda.stream(s_in):
-            for k in names:
+            for k in small:
                 dev[k].copy_(host[k], non_blocking=True)
                 landed[k] = torch.cuda.Event()
                 landed[k].record(s_in)
-        done = {}
         with torch.cuda.stream(s_cmp):
-            for w in order:
+            for w in ("Wmnij", "Wmbej", "E"):
                 for k in inputs_of[w]:
                     s_cmp.wait_event(landed[k])
                 ccd_step(eg, {"t": dev["t"], "g_oovv": dev["g_oovv"]}, W, precision, args.slices, only=w)
                 done[w] = torch.cuda.Event()
                 done[w].record(s_cmp)
         with torch.cuda.stream(s_out):
-            for w in order:
+            for w in ("Wmnij", "Wmbej", "E"):
                 s_out.wait_event(done[w])
                 out[w].copy_(W[w], non_blocking=True)
-            freed.record(s_out)
+        for a0, a1 in bounds:
+            buf, buf_free = slabs[counter[0] % len(slabs)]
+            counter[0] += 1
+            wc = buf[:a1 - a0]
+            s_in.wait_event(buf_free)
+            with torch.cuda.stream(s_in):
+                wc.copy_(host["g_vvvv"][a0:a1], non_blocking=True)
+                ev_in = torch.cuda.Event()
+                ev_in.record(s_in)
+            with torch.cuda.stream(s_cmp):
+                s_cmp.wait_event(ev_in)
+                eg.einsum(1.0, "abef", wc, 0.25, "mnef", dev["g_oovv"], "mnab", dev["t"][:, :, a0:a1, :],
+                          precision=precision, slices=args.slices)
+                ev_c = torch.cuda.Event()
+                ev_c.record(s_cmp)
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(ev_c)
+                out["Wabef"][a0:a1].copy_(wc, non_blocking=True)
+                buf_free.record(s_out)
+        freed.record(s_out)
 
     steps = max(1, min(args.steps, 3)) if precision == "fp64" else args.steps
     for i in range(max(1, args.warmup if precision != "fp64" else 1)):
@@ -452,9 +483,13 @@ def run_e2e(eg, T, precision, args, o, v, step_flops):
     e1.record(s_out)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
-    return {"value": step_flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "ms_per_step": ms, "steps": steps,
-            "pipelining": "two buffer sets; uploads, contractions and read-backs on three streams"}
+    res = {"value": step_flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": ms, "steps": steps,
+           "pipelining": f"uploads, contractions and read-backs on three streams; three sets of the 0.6 GB inputs; "
+                         f"Wabef in {chunks} slabs of rows a through four slab buffers"}
+    if return_outputs:
+        return res, out
+    return res
 
 
 # --------------------------------------------------------- reference arm --

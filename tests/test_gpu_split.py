@@ -166,3 +166,25 @@ def test_deterministic(eg):
         eg.einsum(0.0, "ij", C, 1.0, "ik", A, "kj", B, precision="split_bf16")
         outs.append(C.cpu().numpy())
     assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
+
+
+def test_e2e_slab_pipeline_matches_whole_step(eg):
+    """The host-buffer pipeline moves Wabef in row slabs through a ring of device
+    buffers on three streams; every result must equal the whole-step contraction
+    bit for bit (each element's row, column and K sum are unchanged by slabbing)."""
+    import os
+    import sys
+    import types
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    from einsums_gb300 import workloads
+    o, v = 6, 20
+    T = workloads.ccd_inputs(o, v, seed=5, backend="torch")
+    args = types.SimpleNamespace(steps=4, warmup=1, slices=5)
+    _, out = bench.run_e2e(eg, T, "split_bf16", args, o, v, 1.0, chunks=3, return_outputs=True)
+    W = bench.fresh_W(T)
+    bench.ccd_step(eg, T, W, "split_bf16", 5)
+    torch.cuda.synchronize()
+    for k in ("Wmnij", "Wmbej", "Wabef"):
+        assert torch.equal(out[k], W[k].cpu()), k
+    assert abs(float(out["E"]) - float(W["E"])) <= 1e-14 * max(1.0, abs(float(W["E"])))
