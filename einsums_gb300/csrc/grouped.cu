@@ -162,157 +162,148 @@ struct GOp {
     int64_t rows, Rp, K, Kp;
     int64_t rowbase;      // first entry in the row-max / exponent arrays
     int64_t zbase;        // first digit plane
-    int64_t units_before; // prefix of units (rowmax units for the rowmax table, digit units for the digits table)
+    int64_t rtab, ktab;   // first entries of this operand's row and K offsets in the plan's offset table
 };
-
-constexpr int TT = 32, TR = 8;
-
-__device__ __forceinline__ int find_item(const GOp *ops, int nops, int64_t u) {
-    int lo = 0, hi = nops - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (ops[mid].units_before <= u)
-            lo = mid;
-        else
-            hi = mid - 1;
-    }
-    return lo;
-}
 
 __device__ __forceinline__ int64_t pick(int comp, int64_t oa, int64_t ob) { return comp == 0 ? oa : ob; }
 
-__global__ void __launch_bounds__(TT *TR) k_grouped_rowmax(const GOp *ops, int nops, int64_t total_units,
-                                                           unsigned long long *rowmax) {
-    __shared__ unsigned long long red[TR][TT];
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    for (int64_t u = blockIdx.x; u < total_units; u += gridDim.x) {
-        const GOp &g = ops[find_item(ops, nops, u)];
-        const int64_t local = u - g.units_before;
-        const int64_t rt = (g.rows + TT - 1) / TT, kt = (g.K + TT - 1) / TT;
-        const int64_t ktile = local % kt, rtile = (local / kt) % rt, b = local / (kt * rt);
+// One work unit = 32 rows of one operand of one item (and batch index): the
+// rows' maxima (the operand is read once along its contiguous direction), their
+// exponents, then the digit planes of those rows, written K-major in BF16 pairs
+// through a 32 x 64 shared tile when the operand is contiguous along its rows.
+// Only the real rows and K are written: the planes and exponents of padded rows
+// and of K beyond the item's extent are zeroed once when the plan is built and
+// never written after.
+constexpr int kGU = 32, kGK = 64, kGThreads = 256, kGWarps = kGThreads / 32;
+
+template <int S>
+__global__ void __launch_bounds__(kGThreads) k_grouped_split(const GOp *ops, const int4 *units, int nunits,
+                                                             const long long *__restrict__ offs, int *rexpA,
+                                                             int *rexpB, __nv_bfloat16 *planesA,
+                                                             __nv_bfloat16 *planesB, int64_t Rmax, int64_t Kmaxp) {
+    __shared__ double tile[kGU][kGK + 1];
+    __shared__ unsigned long long red[kGWarps][kGU];
+    __shared__ int ex[kGU];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+        const int4 un = units[u];
+        const GOp &g = ops[un.x];
+        const int64_t b = un.y, r0 = un.z;
+        const int64_t K = g.K;
+        const int nr = (int)(g.rows - r0 < kGU ? g.rows - r0 : kGU);
+        const long long *koff = offs + g.ktab; // element offset of each k in this operand
+        const double *X = g.X;
         int64_t oa, ob, oc;
         group_offsets(g.bg, b, oa, ob, oc);
         const int64_t obase = pick(g.comp, oa, ob);
-        const int64_t r0 = rtile * TT, k0 = ktile * TT;
-        unsigned long long *rm = rowmax + g.rowbase + b * g.Rp;
-        if (g.row_fast) {
-            const int64_t r = r0 + tx;
+        const bool row_fast = g.row_fast != 0;
+        // row offsets: the lane's row (rows contiguous) or the warp's rows w + 8j (K contiguous)
+        int64_t orow[kGU / kGWarps];
+#pragma unroll
+        for (int j = 0; j < kGU / kGWarps; j++) {
+            const int rr = row_fast ? lane : w + kGWarps * j;
+            orow[j] = (rr < nr && (j == 0 || !row_fast)) ? obase + __ldg(offs + g.rtab + r0 + rr) : 0;
+        }
+        // phase 1: row maxima of |x| as IEEE bit patterns
+        if (row_fast) {
             unsigned long long mx = 0;
-            if (r < g.rows) {
-                group_offsets32(g.rg, (uint32_t)r, oa, ob, oc);
-                const int64_t orow = obase + pick(g.comp, oa, ob);
-                for (int j = ty; j < TT; j += TR) {
-                    const int64_t k = k0 + j;
-                    if (k < g.K) {
-                        group_offsets32(g.kg, (uint32_t)k, oa, ob, oc);
-                        mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(g.X + orow + pick(g.comp, oa, ob)))));
+            if (lane < nr) {
+#pragma unroll 4
+                for (int64_t k = w; k < K; k += kGWarps)
+                    mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(X + orow[0] + __ldg(koff + k)))));
+            }
+            red[w][lane] = mx;
+        } else {
+#pragma unroll
+            for (int j = 0; j < kGU / kGWarps; j++) {
+                const int rr = w + kGWarps * j;
+                unsigned long long mx = 0;
+                if (rr < nr) {
+#pragma unroll 4
+                    for (int64_t k = lane; k < K; k += 32)
+                        mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(X + orow[j] + __ldg(koff + k)))));
+                }
+                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                if (lane == 0) {
+                    red[0][rr] = mx;
+                    for (int q = 1; q < kGWarps; q++) red[q][rr] = 0;
+                }
+            }
+        }
+        __syncthreads();
+        if (w == 0) {
+            unsigned long long mx = red[0][lane];
+            for (int q = 1; q < kGWarps; q++) mx = max(mx, red[q][lane]);
+            const double m = __longlong_as_double((long long)mx);
+            int e = 0;
+            if (!isfinite(m))
+                e = INT_MIN;
+            else if (m > 0.0)
+                frexp(m, &e);
+            ex[lane] = e;
+            if (lane < nr) (g.comp ? rexpB : rexpA)[g.rowbase + b * g.Rp + r0 + lane] = e;
+        }
+        __syncthreads();
+        // phase 2: digit planes, 64 K at a time
+        __nv_bfloat16 *planes = g.comp ? planesB : planesA;
+        const int64_t z0 = g.zbase + b * S;
+        for (int64_t k0 = 0; k0 < K; k0 += kGK) {
+            if (row_fast) {
+#pragma unroll 4
+                for (int kk = w; kk < kGK; kk += kGWarps) {
+                    const int64_t k = k0 + kk;
+                    tile[lane][kk] = (k < K && lane < nr) ? __ldg(X + orow[0] + __ldg(koff + k)) : 0.0;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < kGU / kGWarps; j++) {
+                    const int rr = w + kGWarps * j;
+#pragma unroll
+                    for (int h = 0; h < kGK / 32; h++) {
+                        const int64_t k = k0 + lane + 32 * h;
+                        tile[rr][lane + 32 * h] = (rr < nr && k < K) ? __ldg(X + orow[j] + __ldg(koff + k)) : 0.0;
                     }
                 }
             }
-            red[ty][tx] = mx;
             __syncthreads();
-            if (ty == 0) {
-                for (int j = 1; j < TR; j++) mx = max(mx, red[j][tx]);
-                if (r < g.rows && mx) atomicMax(rm + r, mx);
-            }
-            __syncthreads();
-        } else {
-            const int64_t k = k0 + tx;
-            int64_t okk = 0;
-            if (k < g.K) {
-                group_offsets32(g.kg, (uint32_t)k, oa, ob, oc);
-                okk = pick(g.comp, oa, ob);
-            }
-            for (int j = ty; j < TT; j += TR) {
-                const int64_t r = r0 + j;
-                unsigned long long v = 0;
-                if (r < g.rows && k < g.K) {
-                    group_offsets32(g.rg, (uint32_t)r, oa, ob, oc);
-                    v = (unsigned long long)__double_as_longlong(fabs(__ldg(g.X + obase + pick(g.comp, oa, ob) + okk)));
+            const int64_t k = k0 + 2 * lane;
+#pragma unroll
+            for (int j = 0; j < kGU / kGWarps; j++) {
+                const int rr = w + kGWarps * j;
+                if (rr < nr && k < K) {
+                    uint32_t pk[S];
+                    const int e = ex[rr];
+                    if (e == INT_MIN) {
+#pragma unroll
+                        for (int q = 0; q < S; q++) pk[q] = 0u;
+                    } else {
+                        split::digits_bf16x2<S>(tile[rr][2 * lane], tile[rr][2 * lane + 1], e, pk);
+                    }
+#pragma unroll
+                    for (int q = 0; q < S; q++)
+                        *reinterpret_cast<uint32_t *>(planes + ((z0 + q) * Rmax + r0 + rr) * Kmaxp + k) = pk[q];
                 }
-                for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-                if (tx == 0 && r < g.rows && v) atomicMax(rm + r, v);
             }
+            __syncthreads();
         }
     }
 }
 
-__global__ void __launch_bounds__(TT *TR) k_grouped_digits(const GOp *ops, int nops, int64_t total_units,
-                                                           const int *rexp, __nv_bfloat16 *planes, int64_t Rmax,
-                                                           int64_t Kmaxp, int S) {
-    __shared__ double tile[TT][TT + 1];
-    __shared__ int ex[TT];
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    for (int64_t u = blockIdx.x; u < total_units; u += gridDim.x) {
-        const GOp &g = ops[find_item(ops, nops, u)];
-        const int64_t local = u - g.units_before;
-        const int64_t rt = g.Rp / TT, kt = g.Kp / TT;
-        const int64_t ktile = local % kt, rtile = (local / kt) % rt, b = local / (kt * rt);
-        int64_t oa, ob, oc;
-        group_offsets(g.bg, b, oa, ob, oc);
-        const int64_t obase = pick(g.comp, oa, ob);
-        const int64_t r0 = rtile * TT, k0 = ktile * TT;
-        if (ty == 0) ex[tx] = (r0 + tx < g.rows) ? rexp[g.rowbase + b * g.Rp + r0 + tx] : 0;
-        if (g.row_fast) {
-            const int64_t r = r0 + tx;
-            int64_t orow = 0;
-            if (r < g.rows) {
-                group_offsets32(g.rg, (uint32_t)r, oa, ob, oc);
-                orow = obase + pick(g.comp, oa, ob);
-            }
-            for (int j = ty; j < TT; j += TR) {
-                const int64_t k = k0 + j;
-                double v = 0.0;
-                if (r < g.rows && k < g.K) {
-                    group_offsets32(g.kg, (uint32_t)k, oa, ob, oc);
-                    v = __ldg(g.X + orow + pick(g.comp, oa, ob));
-                }
-                tile[tx][j] = v;
-            }
-        } else {
-            const int64_t k = k0 + tx;
-            int64_t okk = 0;
-            if (k < g.K) {
-                group_offsets32(g.kg, (uint32_t)k, oa, ob, oc);
-                okk = pick(g.comp, oa, ob);
-            }
-            for (int j = ty; j < TT; j += TR) {
-                const int64_t r = r0 + j;
-                double v = 0.0;
-                if (r < g.rows && k < g.K) {
-                    group_offsets32(g.rg, (uint32_t)r, oa, ob, oc);
-                    v = __ldg(g.X + obase + pick(g.comp, oa, ob) + okk);
-                }
-                tile[j][tx] = v;
-            }
-        }
-        __syncthreads();
-        for (int j = ty; j < TT; j += TR) {
-            const int64_t r = r0 + j;
-            int dig[split::kMaxSlices];
-            const int e = ex[j];
-            if (e == INT_MIN) {
-                for (int s = 0; s < S; s++) dig[s] = 0;
-            } else {
-                split::to_digits(tile[j][tx], e, S, dig);
-            }
-            const int64_t z0 = g.zbase + b * S;
-            for (int s = 0; s < S; s++)
-                planes[((z0 + s) * Rmax + r) * Kmaxp + k0 + tx] = __float2bfloat16_rn((float)dig[s]);
-        }
-        __syncthreads();
-    }
+template <int S>
+void launch_grouped_split_s(const GOp *ops, const int4 *units, int nunits, const long long *offs, int *eA, int *eB,
+                            __nv_bfloat16 *pA, __nv_bfloat16 *pB, int64_t Rmax, int64_t Kmaxp, cudaStream_t s) {
+    const int grid = (int)std::min<int64_t>(std::max(nunits, 1), (int64_t)num_sms() * 8);
+    k_grouped_split<S><<<grid, kGThreads, 0, s>>>(ops, units, nunits, offs, eA, eB, pA, pB, Rmax, Kmaxp);
 }
 
-__global__ void k_grouped_exponent(const unsigned long long *rowmax, int *e, int64_t n) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double mx = __longlong_as_double((long long)rowmax[i]);
-        int ex = 0;
-        if (!isfinite(mx))
-            ex = INT_MIN;
-        else if (mx > 0.0)
-            frexp(mx, &ex);
-        e[i] = ex;
+void launch_grouped_split(int S, const GOp *ops, const int4 *units, int nunits, const long long *offs, int *eA,
+                          int *eB, __nv_bfloat16 *pA, __nv_bfloat16 *pB, int64_t Rmax, int64_t Kmaxp, cudaStream_t s) {
+    switch (S) {
+    case 2: launch_grouped_split_s<2>(ops, units, nunits, offs, eA, eB, pA, pB, Rmax, Kmaxp, s); break;
+    case 3: launch_grouped_split_s<3>(ops, units, nunits, offs, eA, eB, pA, pB, Rmax, Kmaxp, s); break;
+    case 4: launch_grouped_split_s<4>(ops, units, nunits, offs, eA, eB, pA, pB, Rmax, Kmaxp, s); break;
+    case 5: launch_grouped_split_s<5>(ops, units, nunits, offs, eA, eB, pA, pB, Rmax, Kmaxp, s); break;
+    default: launch_grouped_split_s<6>(ops, units, nunits, offs, eA, eB, pA, pB, Rmax, Kmaxp, s); break;
     }
 }
 
@@ -547,8 +538,7 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     std::vector<GOp> opsA, opsB;
     std::vector<TcItem> items;
     std::vector<std::pair<int64_t, int4>> work;
-    int64_t unitsA = 0, unitsB = 0, dunitsA = 0, dunitsB = 0;
-    std::vector<int64_t> dprefA, dprefB;
+    std::vector<int4> units; // (operand, batch index, first row); operands A then B of every item
     for (size_t i = 0; i < cs.size(); i++) {
         const Contraction &c = cs[i];
         const int64_t nb = c.batch.total, M = c.m.total, N = c.n.total, K = c.k.total;
@@ -567,7 +557,6 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
         a.Kp = Kp;
         a.rowbase = rowsA;
         a.zbase = zA;
-        a.units_before = unitsA;
         GOp b = a;
         b.X = c.B;
         b.rg = c.n;
@@ -577,15 +566,8 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
         b.Rp = Np;
         b.rowbase = rowsB;
         b.zbase = zB;
-        b.units_before = unitsB;
         opsA.push_back(a);
         opsB.push_back(b);
-        dprefA.push_back(dunitsA);
-        dprefB.push_back(dunitsB);
-        unitsA += nb * ((M + 31) / 32) * ((K + 31) / 32);
-        unitsB += nb * ((N + 31) / 32) * ((K + 31) / 32);
-        dunitsA += nb * (Mp / 32) * (Kp / 32);
-        dunitsB += nb * (Np / 32) * (Kp / 32);
         TcItem it{};
         it.C = c.C;
         it.M = M;
@@ -615,26 +597,45 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     std::stable_sort(work.begin(), work.end(), [](auto &x, auto &y) { return x.first > y.first; });
     std::vector<int4> wl;
     for (auto &w : work) wl.push_back(w.second);
-    // digit-unit prefixes replace the rowmax prefixes in the digit tables
-    std::vector<GOp> dopsA = opsA, dopsB = opsB;
-    for (size_t i = 0; i < cs.size(); i++) {
-        dopsA[i].units_before = dprefA[i];
-        dopsB[i].units_before = dprefB[i];
+    // one splitting unit per 32 real rows of every operand (and batch index)
+    std::vector<GOp> ops(opsA);
+    ops.insert(ops.end(), opsB.begin(), opsB.end());
+    // row and K element offsets of every operand, fixed by the strides: built once here
+    std::vector<long long> offs;
+    for (auto &op : ops) {
+        int64_t oa, ob, oc;
+        op.rtab = (int64_t)offs.size();
+        for (int64_t r = 0; r < op.rows; r++) {
+            group_offsets(op.rg, r, oa, ob, oc);
+            offs.push_back(op.comp ? ob : oa);
+        }
+        op.ktab = (int64_t)offs.size();
+        for (int64_t k = 0; k < op.K; k++) {
+            group_offsets(op.kg, k, oa, ob, oc);
+            offs.push_back(op.comp ? ob : oa);
+        }
     }
+    for (size_t i = 0; i < ops.size(); i++)
+        for (int64_t bb = 0; bb < ops[i].nbatch; bb++)
+            for (int64_t r0 = 0; r0 < ops[i].rows; r0 += 32) units.push_back(make_int4((int)i, (int)bb, (int)r0, 0));
+    if (units.size() >= (size_t)INT_MAX) return fail(EG_ERROR_NOT_SUPPORTED, "grouped split: batch too large");
 
-    void *planesA, *planesB, *maxA, *maxB, *eA, *eB, *d_opsA, *d_opsB, *d_dopsA, *d_dopsB, *d_items, *d_work, *rbuf;
+    void *planesA, *planesB, *eA, *eB, *d_ops, *d_units, *d_offs, *d_items, *d_work, *rbuf;
     eg_status st;
     if ((st = dev_alloc(plan, rbuf_bytes(), &rbuf)) != EG_SUCCESS) return st;
-    if ((st = dev_alloc(plan, (size_t)zA * Rmax * Kmaxp * 2, &planesA)) != EG_SUCCESS) return st;
-    if ((st = dev_alloc(plan, (size_t)zB * Rmax * Kmaxp * 2, &planesB)) != EG_SUCCESS) return st;
-    if ((st = dev_alloc(plan, (size_t)rowsA * 8, &maxA)) != EG_SUCCESS) return st;
-    if ((st = dev_alloc(plan, (size_t)rowsB * 8, &maxB)) != EG_SUCCESS) return st;
+    const size_t pbytesA = (size_t)zA * Rmax * Kmaxp * 2, pbytesB = (size_t)zB * Rmax * Kmaxp * 2;
+    if ((st = dev_alloc(plan, pbytesA, &planesA)) != EG_SUCCESS) return st;
+    if ((st = dev_alloc(plan, pbytesB, &planesB)) != EG_SUCCESS) return st;
     if ((st = dev_alloc(plan, (size_t)rowsA * 4, &eA)) != EG_SUCCESS) return st;
     if ((st = dev_alloc(plan, (size_t)rowsB * 4, &eB)) != EG_SUCCESS) return st;
-    if ((st = dev_copy(plan, opsA.data(), opsA.size() * sizeof(GOp), &d_opsA)) != EG_SUCCESS) return st;
-    if ((st = dev_copy(plan, opsB.data(), opsB.size() * sizeof(GOp), &d_opsB)) != EG_SUCCESS) return st;
-    if ((st = dev_copy(plan, dopsA.data(), dopsA.size() * sizeof(GOp), &d_dopsA)) != EG_SUCCESS) return st;
-    if ((st = dev_copy(plan, dopsB.data(), dopsB.size() * sizeof(GOp), &d_dopsB)) != EG_SUCCESS) return st;
+    // padded rows and K are never written by the splitting kernel: zero them once
+    EG_CUDA(cudaMemsetAsync(planesA, 0, pbytesA, s));
+    EG_CUDA(cudaMemsetAsync(planesB, 0, pbytesB, s));
+    EG_CUDA(cudaMemsetAsync(eA, 0, (size_t)rowsA * 4, s));
+    EG_CUDA(cudaMemsetAsync(eB, 0, (size_t)rowsB * 4, s));
+    if ((st = dev_copy(plan, ops.data(), ops.size() * sizeof(GOp), &d_ops)) != EG_SUCCESS) return st;
+    if ((st = dev_copy(plan, units.data(), units.size() * sizeof(int4), &d_units)) != EG_SUCCESS) return st;
+    if ((st = dev_copy(plan, offs.data(), offs.size() * sizeof(long long), &d_offs)) != EG_SUCCESS) return st;
     if ((st = dev_copy(plan, items.data(), items.size() * sizeof(TcItem), &d_items)) != EG_SUCCESS) return st;
     if ((st = dev_copy(plan, wl.data(), wl.size() * sizeof(int4), &d_work)) != EG_SUCCESS) return st;
 
@@ -667,26 +668,14 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     p.kslice = 0;
     p.rbuf = (long long *)rbuf;
 
-    const int cap = num_sms() * 16;
     if ((st = ensure_tc_attributes()) != EG_SUCCESS) return st;
     EG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     {
         CaptureGuard g;
         auto issue = [&]() -> eg_status {
-            EG_CUDA(cudaMemsetAsync(maxA, 0, (size_t)rowsA * 8, s));
-            EG_CUDA(cudaMemsetAsync(maxB, 0, (size_t)rowsB * 8, s));
-            k_grouped_rowmax<<<(int)std::min<int64_t>(std::max<int64_t>(unitsA, 1), cap), dim3(TT, TR), 0, s>>>(
-                (GOp *)d_opsA, (int)cs.size(), unitsA, (unsigned long long *)maxA);
-            k_grouped_rowmax<<<(int)std::min<int64_t>(std::max<int64_t>(unitsB, 1), cap), dim3(TT, TR), 0, s>>>(
-                (GOp *)d_opsB, (int)cs.size(), unitsB, (unsigned long long *)maxB);
-            k_grouped_exponent<<<(int)std::min<int64_t>((rowsA + 255) / 256 + 1, cap), 256, 0, s>>>(
-                (unsigned long long *)maxA, (int *)eA, rowsA);
-            k_grouped_exponent<<<(int)std::min<int64_t>((rowsB + 255) / 256 + 1, cap), 256, 0, s>>>(
-                (unsigned long long *)maxB, (int *)eB, rowsB);
-            k_grouped_digits<<<(int)std::min<int64_t>(std::max<int64_t>(dunitsA, 1), cap), dim3(TT, TR), 0, s>>>(
-                (GOp *)d_dopsA, (int)cs.size(), dunitsA, (int *)eA, (__nv_bfloat16 *)planesA, Rmax, Kmaxp, S);
-            k_grouped_digits<<<(int)std::min<int64_t>(std::max<int64_t>(dunitsB, 1), cap), dim3(TT, TR), 0, s>>>(
-                (GOp *)d_dopsB, (int)cs.size(), dunitsB, (int *)eB, (__nv_bfloat16 *)planesB, Rmax, Kmaxp, S);
+            launch_grouped_split(S, (const GOp *)d_ops, (const int4 *)d_units, (int)units.size(),
+                                 (const long long *)d_offs, (int *)eA, (int *)eB,
+                                 (__nv_bfloat16 *)planesA, (__nv_bfloat16 *)planesB, Rmax, Kmaxp, s);
             EG_CHECK_LAUNCH("grouped digit splitting");
             return launch_tc_gemm_grouped(tmA, tmB, p, (TcItem *)d_items, (int4 *)d_work, (int)wl.size(), s);
         };
@@ -701,7 +690,7 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     if (err != cudaSuccess) return cuda_fail(err, "cudaStreamEndCapture");
     plan.graph = graph;
     EG_CUDA(cudaGraphInstantiate(&plan.exec, graph, 0));
-    plan.kernels = 7;
+    plan.kernels = 2;
     plan.report = eg_split_report{S, S * (S + 1) / 2, kBits, error_bound(S)};
     return EG_SUCCESS;
 }

@@ -207,19 +207,17 @@ __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const doub
 #pragma unroll
         for (int j = ty; j < T; j += TR) {
             const int64_t r = r0 + j;
-            int d0[S], d1[S];
+            uint32_t pk[S];
             const int e = ex[j];
             if (e == INT_MIN) {
 #pragma unroll
-                for (int s = 0; s < S; s++) d0[s] = d1[s] = 0;
+                for (int s = 0; s < S; s++) pk[s] = 0u;
             } else {
-                to_digits(tile[j][2 * tx], e, S, d0);
-                to_digits(tile[j][2 * tx + 1], e, S, d1);
+                digits_bf16x2<S>(tile[j][2 * tx], tile[j][2 * tx + 1], e, pk);
             }
-            __nv_bfloat162 *out = (__nv_bfloat162 *)(planes + ((int64_t)b * S) * plane + r * m.Kp + k0) + tx;
+            uint32_t *out = (uint32_t *)(planes + ((int64_t)b * S) * plane + r * m.Kp + k0) + tx;
 #pragma unroll
-            for (int s = 0; s < S; s++)
-                out[(int64_t)s * (plane / 2)] = __floats2bfloat162_rn((float)d0[s], (float)d1[s]);
+            for (int s = 0; s < S; s++) out[(int64_t)s * (plane / 2)] = pk[s];
         }
         __syncthreads();
         }

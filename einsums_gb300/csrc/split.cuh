@@ -121,6 +121,37 @@ __device__ __forceinline__ void to_digits(double x, int e, int S, int *dig) {
     dig[0] = (int)F;
 }
 
+// The digits of two values as BF16 pairs: out[s] holds digit s of x0 in its low
+// half and digit s of x1 in its high half — the same digits as to_digits.  With
+// B = 127 (256^(S-2) + ... + 256 + 1), G = F + B has the ordinary base-256
+// digits d_s + 127 in [0, 255] for s >= 1 and G >> 8(S-1) = d_0, so one 64-bit
+// add replaces the subtract-and-shift chain.  A byte u becomes the float u - 127
+// exactly as (2^23 + u) - (2^23 + 127) (bit OR, then an FP32 add), and d_0 as
+// (1.5 * 2^23 + d_0) - 1.5 * 2^23; every digit has at most 8 significant bits,
+// so its BF16 is the float's upper half, and one byte permute packs the pair.
+template <int S>
+__device__ __forceinline__ void digits_bf16x2(double x0, double x1, int e, uint32_t *out) {
+    constexpr long long bias = [] {
+        long long b = 0;
+        for (int s = 1; s < S; s++) b = b * 256 + 127;
+        return b;
+    }();
+    const int sh = kTopBits + kBits * (S - 1) - e;
+    const long long G0 = scaled_round(x0, sh) + bias, G1 = scaled_round(x1, sh) + bias;
+#pragma unroll
+    for (int s = 1; s < S; s++) {
+        const int p = 8 * (S - 1 - s);
+        const uint32_t u0 = (uint32_t)(G0 >> p) & 255u, u1 = (uint32_t)(G1 >> p) & 255u;
+        const float f0 = __uint_as_float(0x4B000000u | u0) - 8388735.0f;
+        const float f1 = __uint_as_float(0x4B000000u | u1) - 8388735.0f;
+        out[s] = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
+    }
+    const int t0 = (int)(G0 >> (8 * (S - 1))), t1 = (int)(G1 >> (8 * (S - 1)));
+    const float f0 = __int_as_float(0x4B400000 + t0) - 12582912.0f;
+    const float f1 = __int_as_float(0x4B400000 + t1) - 12582912.0f;
+    out[0] = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
+}
+
 // Sets the kernels' shared-memory attribute once (call outside stream capture).
 eg_status ensure_tc_attributes();
 // tmBh: the B planes with a 64-row box (half a tile), used when two CTAs of a

@@ -99,3 +99,30 @@ def test_autotuner_cache_written(eg):
     assert os.path.exists(path)
     lines = open(path).read().strip().split("\n")
     assert any("|f64|" in l and l.rsplit("=", 1)[1] in ("32", "64") for l in lines)
+
+
+@pytest.mark.parametrize("pattern", [("ab", "ai", "ib"), ("zab", "zai", "zbi"), ("ab", "ia", "bi")])
+def test_grouped_split_operand_layouts(eg, pattern):
+    """Operands contiguous along K, along their rows, and with a batch index;
+    odd K, rows spanning several 32-row splitting units and two row tiles."""
+    Cl, Al, Bl = pattern
+    rng = np.random.default_rng(17)
+    dims_list = [dict(z=2, a=7, b=33, i=5), dict(z=1, a=150, b=64, i=129), dict(z=3, a=40, b=200, i=300),
+                 dict(z=2, a=3, b=5, i=2), dict(z=1, a=65, b=97, i=64)]
+    As, Bs, Cs0 = [], [], []
+    for d in dims_list:
+        As.append(rng.standard_normal([d[c] for c in Al]) * 10.0 ** rng.integers(-3, 3))
+        Bs.append(rng.standard_normal([d[c] for c in Bl]))
+        Cs0.append(rng.standard_normal([d[c] for c in Cl]))
+    tA, tB, tC = [cu(x) for x in As], [cu(x) for x in Bs], [cu(x) for x in Cs0]
+    plan = eg.GroupedPlan(0.5, Cl, tC, 2.0, Al, tA, Bl, tB, precision="split_bf16")
+    for _ in range(2):  # a replay rewrites the digit planes from the current inputs
+        for k in range(len(tC)):
+            tC[k].copy_(cu(Cs0[k]))
+        plan.execute()
+        torch.cuda.synchronize()
+        for k in range(len(As)):
+            ref = Cs0[k].copy()
+            oracle.einsum(Cl, ref, 0.5, 2.0, Al, As[k], Bl, Bs[k])
+            assert oracle.rel_fro(tC[k].cpu().numpy(), ref) < 1e-10, k
+    plan.close()

@@ -188,3 +188,32 @@ def test_e2e_slab_pipeline_matches_whole_step(eg):
     for k in ("Wmnij", "Wmbej", "Wabef"):
         assert torch.equal(out[k], W[k].cpu()), k
     assert abs(float(out["E"]) - float(W["E"])) <= 1e-14 * max(1.0, abs(float(W["E"])))
+
+
+@pytest.mark.parametrize("S,K", [(3, 300), (4, 257), (5, 1000), (5, 70), (6, 128)])
+def test_split_result_is_the_exact_split_product(eg, S, K):
+    """Digits, exact integer accumulation and the final int64 -> FP64 rounding
+    together: C = A B^T through the split path equals, bit for bit, the CPU
+    restatement of the scheme with Python integers (one exact pass of K)."""
+    from test_split_math import split_product
+    rng = np.random.default_rng(100 + S)
+    M, N = 37, 130
+    A = rng.standard_normal((M, K)) * np.exp2(rng.integers(-20, 20, size=(M, 1)))
+    B = rng.standard_normal((N, K))
+    A[3, :] = 0.0  # a zero row
+    ref = split_product(A, B, S)
+    C = torch.zeros((M, N), dtype=torch.float64, device="cuda")
+    eg.einsum(0.0, "ij", C, 1.0, "ik", cu(A), "jk", cu(B), precision="split_bf16", slices=S)
+    assert eg.last_split_report()["slices"] == S
+    assert np.array_equal(C.cpu().numpy().view(np.uint64), ref.view(np.uint64))
+    # the grouped launch computes every item the same way
+    As = [A, A[:20, :]]
+    Bs = [B, B[:9, :]]
+    Cs = [torch.zeros((a.shape[0], b.shape[0]), dtype=torch.float64, device="cuda") for a, b in zip(As, Bs)]
+    plan = eg.GroupedPlan(0.0, "ij", Cs, 1.0, "ik", [cu(a) for a in As], "jk", [cu(b) for b in Bs],
+                          precision="split_bf16", slices=S)
+    plan.execute()
+    torch.cuda.synchronize()
+    for a, b, c in zip(As, Bs, Cs):
+        assert np.array_equal(c.cpu().numpy().view(np.uint64), split_product(a, b, S).view(np.uint64))
+    plan.close()
