@@ -3,6 +3,7 @@
 // eg_grouped_plan_execute replays it.  eg_einsum_batched keeps a small cache
 // of plans keyed by a hash of the call (pattern, prefactors, options, and
 // every item's pointers, extents and strides), so a repeated call replays.
+#include <cstdio>
 #include <cstring>
 #include <list>
 #include <map>
@@ -27,21 +28,6 @@ struct eg_grouped_plan {
     std::unique_ptr<eg::grouped::Plan> plan;
 };
 
-namespace eg::grouped {
-struct Plan {
-    int device = 0;
-    int precision = EG_PRECISION_FP64;
-    int slices = 0;
-    int64_t count = 0;
-    int32_t algorithm = 0;
-    std::vector<void *> owned;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    uint64_t kernels = 0;
-    eg_split_report report{};
-    ~Plan();
-};
-} // namespace eg::grouped
 
 namespace {
 
@@ -133,6 +119,23 @@ eg_status run_plan(Plan &plan, cudaStream_t stream) {
 
 namespace eg::grouped {
 Plan::~Plan() {
+    if (prof) {
+        // tracing aid (EINSUMS_GB300_TC_PROFILE): the tensor kernel's per-role cycles over all replays
+        std::vector<unsigned long long> h((size_t)num_sms() * 8);
+        if (cudaMemcpy(h.data(), prof, h.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess) {
+            double tot[8] = {0};
+            int ran = 0;
+            for (size_t i = 0; i < h.size(); i++) tot[i % 8] += (double)h[i];
+            for (size_t i = 6; i < h.size(); i += 8) ran += h[i] > 0 ? 1 : 0;
+            if (tot[6] > 0)
+                std::fprintf(stderr,
+                             "[tc profile grouped] items=%lld: total %.3g cyc/CTA | producer wait empty %.1f%% | mma wait "
+                             "full %.1f%% | mma wait acc %.1f%% | epi wait acc %.1f%% | epi flush %.1f%% | epi final "
+                             "%.1f%%\n",
+                             (long long)count, tot[6] / (ran > 0 ? ran : 1), 100 * tot[0] / tot[6], 100 * tot[1] / tot[6],
+                             100 * tot[2] / tot[6], 100 * tot[3] / tot[6], 100 * tot[4] / tot[6], 100 * tot[5] / tot[6]);
+        }
+    }
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     for (void *p : owned) tracked_free(p);

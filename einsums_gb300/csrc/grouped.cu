@@ -14,6 +14,8 @@
 //     tcgen05 GEMM over the work list (k_tc_split_gemm<true>).
 #include <algorithm>
 #include <climits>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -314,19 +316,6 @@ bool fast_along(const ModeGroup &g, int comp) { return g.n > 0 && g.s[comp][g.n 
 } // namespace
 
 // ------------------------------------------------------------------ plan --
-struct Plan {
-    int device = 0;
-    int precision = EG_PRECISION_FP64;
-    int slices = 0;
-    int64_t count = 0;
-    int32_t algorithm = 0;
-    std::vector<void *> owned; // device buffers owned by the plan
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    uint64_t kernels = 0; // kernels in one replay
-    eg_split_report report{};
-    ~Plan();
-};
 
 namespace {
 
@@ -667,6 +656,16 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     p.ksplit = 1; // no K slicing in grouped launches
     p.kslice = 0;
     p.rbuf = (long long *)rbuf;
+    static const bool prof_on = std::getenv("EINSUMS_GB300_TC_PROFILE") != nullptr;
+    if (prof_on) {
+        // per-role cycle counters summed over the plan's replays, printed when it is destroyed
+        void *prof = nullptr;
+        const size_t pbytes = (size_t)num_sms() * 8 * sizeof(unsigned long long);
+        if ((st = dev_alloc(plan, pbytes, &prof)) != EG_SUCCESS) return st;
+        EG_CUDA(cudaMemsetAsync(prof, 0, pbytes, s));
+        p.prof = (unsigned long long *)prof;
+        plan.prof = p.prof;
+    }
 
     if ((st = ensure_tc_attributes()) != EG_SUCCESS) return st;
     EG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));

@@ -19,7 +19,23 @@ std::string cache_path();
 } // namespace eg::autotune
 
 namespace eg::grouped {
-struct Plan;
+// A captured grouped launch: the graph, the device buffers it reads (owned), and
+// what it reports.
+struct Plan {
+    int device = 0;
+    int precision = EG_PRECISION_FP64;
+    int slices = 0;
+    int64_t count = 0;
+    int32_t algorithm = 0;
+    std::vector<void *> owned; // device buffers owned by the plan
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t kernels = 0; // kernels in one replay
+    eg_split_report report{};
+    // per-role cycle counters of the tensor kernel, summed over replays (EINSUMS_GB300_TC_PROFILE)
+    unsigned long long *prof = nullptr;
+    ~Plan();
+};
 eg_status build_f64_plan(Plan &plan, const std::vector<Contraction> &cs, cudaStream_t s);
 eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int slices, cudaStream_t s);
 eg_status choose_f64_tiles(const std::vector<Contraction> &cs, cudaStream_t s, std::vector<int> &tiles);
