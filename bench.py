@@ -735,7 +735,12 @@ def run_suite(args):
     sizes = tuple(int(x) for x in args.sizes.split(",")) if args.sizes else None
     for name in which:
         t0 = time.perf_counter()
-        r = fns[name](eg, sizes) if (sizes and name in ("permute", "contraction")) else fns[name](eg)
+        if sizes and name in ("permute", "contraction"):
+            r = fns[name](eg, sizes)
+        elif name == "batched" and args.items:
+            r = fns[name](eg, count=args.items)
+        else:
+            r = fns[name](eg)
         r["suite"] = name
         r["wall_s"] = time.perf_counter() - t0
         print(json.dumps(r), flush=True)
@@ -756,6 +761,7 @@ def main():
                     help="measure the other configurations instead (all, or a comma list of "
                          "fock,permute,contraction,batched,autograd); one JSON line each")
     ap.add_argument("--sizes", default=None, help="extents for the permute / contraction sweeps, e.g. 64,128")
+    ap.add_argument("--items", type=int, default=0, help="contractions in the batched suite (default 2048)")
     args = ap.parse_args()
     if args.suite:
         run_suite(args)

@@ -179,7 +179,7 @@ __device__ __forceinline__ int64_t pick(int comp, int64_t oa, int64_t ob) { retu
 constexpr int kGU = 32, kGK = 64, kGThreads = 256, kGWarps = kGThreads / 32;
 
 template <int S>
-__global__ void __launch_bounds__(kGThreads) k_grouped_split(const GOp *ops, const int4 *units, int nunits,
+__global__ void __launch_bounds__(kGThreads, 4) k_grouped_split(const GOp *ops, const int4 *units, int nunits,
                                                              const long long *__restrict__ offs, int *rexpA,
                                                              int *rexpB, __nv_bfloat16 *planesA,
                                                              __nv_bfloat16 *planesB, int64_t Rmax, int64_t Kmaxp) {
@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(kGThreads) k_grouped_split(const GOp *ops, con
         if (row_fast) {
             unsigned long long mx = 0;
             if (lane < nr) {
-#pragma unroll 4
+#pragma unroll 8
                 for (int64_t k = w; k < K; k += kGWarps)
                     mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(X + orow[0] + __ldg(koff + k)))));
             }
@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(kGThreads) k_grouped_split(const GOp *ops, con
         const int64_t z0 = g.zbase + b * S;
         for (int64_t k0 = 0; k0 < K; k0 += kGK) {
             if (row_fast) {
-#pragma unroll 4
+#pragma unroll
                 for (int kk = w; kk < kGK; kk += kGWarps) {
                     const int64_t k = k0 + kk;
                     tile[lane][kk] = (k < K && lane < nr) ? __ldg(X + orow[0] + __ldg(koff + k)) : 0.0;
