@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(kGThreads, 4) k_grouped_split(const GOp *ops, 
             if (lane < nr) {
 #pragma unroll 8
                 for (int64_t k = w; k < K; k += kGWarps)
-                    mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(X + orow[0] + __ldg(koff + k)))));
+                    mx = max(mx, split::abs_bits(__ldg(X + orow[0] + __ldg(koff + k))));
             }
             red[w][lane] = mx;
         } else {
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(kGThreads, 4) k_grouped_split(const GOp *ops, 
                 if (rr < nr) {
 #pragma unroll 4
                     for (int64_t k = lane; k < K; k += 32)
-                        mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(X + orow[j] + __ldg(koff + k)))));
+                        mx = max(mx, split::abs_bits(__ldg(X + orow[j] + __ldg(koff + k))));
                 }
                 for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
                 if (lane == 0) {

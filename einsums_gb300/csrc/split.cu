@@ -45,6 +45,10 @@ struct OperandMap {
     // or null: then each offset is decomposed mode by mode, which costs integer
     // divisions per element and made these kernels ALU-bound.
     const int64_t *offr = nullptr, *offk = nullptr;
+    // When a group walks memory with a single stride (the usual case: its modes
+    // are nested like a row-major block), that stride; the offset is then
+    // index * stride, with no table load in the dependency chain.  0 otherwise.
+    int64_t sr = 0, sk = 0;
 };
 
 __device__ __forceinline__ int64_t comp_of(int comp, int64_t oa, int64_t ob) { return comp == 0 ? oa : ob; }
@@ -65,9 +69,11 @@ __device__ __forceinline__ int64_t decompose_k(const OperandMap &m, int64_t k) {
     return comp_of(m.comp, oa, ob);
 }
 __device__ __forceinline__ int64_t off_r(const OperandMap &m, int64_t r) {
+    if (m.sr) return r * m.sr;
     return m.offr ? __ldg(m.offr + r) : decompose_r(m, r);
 }
 __device__ __forceinline__ int64_t off_k(const OperandMap &m, int64_t k) {
+    if (m.sk) return k * m.sk;
     return m.offk ? __ldg(m.offk + k) : decompose_k(m, k);
 }
 
@@ -103,7 +109,7 @@ __global__ void __launch_bounds__(T *TR, 5) k_split_rowmax(OperandMap m, const d
                 const double *xr = X + ob + off_r(m, r);
 #pragma unroll 4
                 for (int64_t k = kbeg + ty; k < kend; k += TR)
-                    mx = max(mx, (unsigned long long)__double_as_longlong(fabs(__ldg(xr + off_k(m, k)))));
+                    mx = max(mx, abs_bits(__ldg(xr + off_k(m, k))));
             }
             red[ty][tx] = mx;
             __syncthreads();
@@ -128,7 +134,7 @@ __global__ void __launch_bounds__(T *TR, 5) k_split_rowmax(OperandMap m, const d
                 const int64_t okk = off_k(m, k);
 #pragma unroll
                 for (int j = 0; j < RPT; j++)
-                    if (xr[j]) mx[j] = max(mx[j], (unsigned long long)__double_as_longlong(fabs(__ldg(xr[j] + okk))));
+                    if (xr[j]) mx[j] = max(mx[j], abs_bits(__ldg(xr[j] + okk)));
             }
 #pragma unroll
             for (int j = 0; j < RPT; j++) {
@@ -225,8 +231,18 @@ __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const doub
 }
 
 // K chunk (a multiple of T) giving about eight work units per SM.
-int chunk_for(int64_t units_per_chunk_row, int64_t ktiles) {
-    const int64_t target = (int64_t)num_sms() * 8;
+// CTAs of `kernel` (256 threads, static shared memory) that fit on the GPU at
+// once: the splitting kernels launch exactly one wave of them and loop over
+// their work units, so no partial second wave trails the launch.
+template <typename F>
+int resident_grid(F kernel) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, T * TR, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    return per_sm * num_sms();
+}
+
+// K chunk (a multiple of T) giving about `target` work units.
+int chunk_for(int64_t units_per_chunk_row, int64_t ktiles, int64_t target) {
     const int64_t per_unit = std::max<int64_t>(1, (units_per_chunk_row * ktiles + target - 1) / target);
     return (int)(std::min<int64_t>(per_unit, ktiles) * T);
 }
@@ -265,9 +281,31 @@ int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 bool is_fast(const ModeGroup &g, int comp) { return g.n > 0 && g.s[comp][g.n - 1] == 1; }
 
+// The single stride of a group whose modes (extent-1 modes ignored) nest like a
+// row-major block in operand `comp`, else 0.
+int64_t affine_stride(const ModeGroup &g, int comp) {
+    int64_t stride = 0, span = 0; // stride of the fastest mode seen, and stride * extents so far
+    for (int d = g.n - 1; d >= 0; d--) {
+        if (g.ext[d] == 1) continue;
+        const int64_t sd = g.s[comp][d];
+        if (stride == 0) {
+            if (sd == 0) return 0;
+            stride = sd;
+            span = sd * g.ext[d];
+        } else {
+            if (sd != span) return 0;
+            span = sd * g.ext[d];
+        }
+    }
+    return stride == 0 ? 1 : stride; // no mode of extent > 1: the group has one index, offset 0
+}
+
 eg_status split_operand(OperandMap om, const double *X, unsigned long long *rowmax, int *rexp,
                         __nv_bfloat16 *planes, int S, cudaStream_t s, int64_t *offr, int64_t *offk) {
     const bool k_fast = is_fast(om.kg, om.comp);
+    om.sr = affine_stride(om.rg, om.comp);
+    om.sk = affine_stride(om.kg, om.comp);
+    if (om.sr && om.sk) offr = offk = nullptr; // no tables needed
     if (offr && offk) {
         const int64_t n = std::max(om.rows, om.K);
         {
@@ -283,10 +321,12 @@ eg_status split_operand(OperandMap om, const double *X, unsigned long long *rowm
     EG_CUDA(cudaMemsetAsync(rowmax, 0, (size_t)om.nbatch * om.Rp * sizeof(unsigned long long), s));
     const int cap = num_sms() * 8;
     {
+        static const int resident = resident_grid(k_split_rowmax);
+        // about four units per resident CTA: one wave, balanced
         const int64_t rows_units = (int64_t)om.nbatch * ((om.rows + T - 1) / T);
-        const int kchunk = chunk_for(rows_units, (om.K + T - 1) / T);
+        const int kchunk = chunk_for(rows_units, (om.K + T - 1) / T, 4 * (int64_t)resident);
         const int64_t work = rows_units * ((om.K + kchunk - 1) / kchunk);
-        const int grid = (int)(work < cap ? (work < 1 ? 1 : work) : cap);
+        const int grid = (int)(work < resident ? (work < 1 ? 1 : work) : resident);
         LaunchScope ls_("k_split_rowmax", s);
         k_split_rowmax<<<grid, dim3(T, TR), 0, s>>>(om, X, rowmax, r_fast ? 1 : 0, kchunk);
     }
@@ -299,7 +339,8 @@ eg_status split_operand(OperandMap om, const double *X, unsigned long long *rowm
     EG_CHECK_LAUNCH("k_split_exponent");
     {
         const int64_t work = (int64_t)om.nbatch * (om.Rp / T) * ((om.Kp / TK + kDigitStrip - 1) / kDigitStrip);
-        const int grid = (int)(work < 2 * cap ? work : 2 * cap);
+        static const int resident = resident_grid(k_split_digits<5>); // the S variants share a register budget
+        const int grid = (int)(work < resident ? work : resident);
         LaunchScope ls_("k_split_digits", s);
         const int rf = r_fast ? 1 : 0;
         switch (S) {

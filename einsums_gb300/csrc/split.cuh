@@ -79,6 +79,13 @@ struct TcItem {
     ModeGroup bg, mg, ng;
 };
 
+// IEEE bit pattern of |x|: for non-negative doubles (and NaN above Inf) the
+// unsigned order of the patterns is the numeric order.  Integer ops only: an
+// FP64 abs would run on this GPU's slow FP64 pipe, once per element.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+
 // round(x * 2^sh) to nearest, ties to even, for |x| 2^sh < 2^52, built from the
 // IEEE fields with integer operations (the FP64 pipe of this GPU runs about two
 // operations per clock per SM; this is the splitting kernels' inner loop).
