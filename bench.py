@@ -222,6 +222,21 @@ def host_cores():
         return os.cpu_count() or 1
 
 
+def reduce_max_ms(ms, world, device):
+    """Max over ranks of a per-rank time: the job is as slow as its slowest rank."""
+    if world == 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_tflops(step_flops, ms, world):
+    """Whole-job throughput: every rank processed one step of ``step_flops`` per ``ms``."""
+    return world * step_flops / (ms * 1e-3) / 1e12
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -311,14 +326,11 @@ def run_ours(args, rank, world):
             name, cnt, tot = line.split(",")
             kernels[name] = {"launches": int(cnt), "total_ms": float(tot)}
 
-    if world > 1:
-        t_ms = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t_ms, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t_ms.item())
+    ms = reduce_max_ms(ms, world, "cuda")
 
     per_contraction = {k: sum(a.elapsed_time(b) for a, b in vals) / len(vals) for k, vals in timers.items()}
     per_contraction_fp64 = {k: sum(a.elapsed_time(b) for a, b in vals) / len(vals) for k, vals in fp64_timers.items()}
-    value = world * step_flops / (ms * 1e-3) / 1e12
+    value = job_tflops(step_flops, ms, world)
     fp64_value = step_flops / (ms_fp64 * 1e-3) / 1e12
 
     # Dominant kernel roofline.
@@ -359,9 +371,8 @@ def run_ours(args, rank, world):
                     "peak_source": "fp64 measured live (max of DFMA and DMMA probes)"}
 
     # End to end through the public API: host inputs in, host results out.
-    e2e = None
-    if rank == 0:
-        e2e = run_e2e(eg, T, headline, args, o, v, step_flops)
+    # every rank runs it (replicas), timed between barriers; the slowest rank sets the time
+    e2e = run_e2e(eg, T, headline, args, o, v, step_flops, world=world)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -390,7 +401,7 @@ def run_ours(args, rank, world):
         print(json.dumps(line))
 
 
-def run_e2e(eg, T, precision, args, o, v, step_flops, chunks=8, return_outputs=False):
+def run_e2e(eg, T, precision, args, o, v, step_flops, chunks=8, return_outputs=False, world=1):
     """Same step through the public API with host buffers: every step copies all
     of its inputs in from pinned host memory and all four results back, inside
     the timed region.  The copies are pipelined the way a caller of the API
@@ -406,7 +417,9 @@ def run_e2e(eg, T, precision, args, o, v, step_flops, chunks=8, return_outputs=F
       the K sum are unchanged), so the slabs reproduce it bit for bit.
 
     A set or slab buffer is refilled only after the read-back of its previous
-    contents has finished."""
+    contents has finished.  With several ranks (replicas) every rank runs this
+    between barriers; the slowest rank's time and all ranks' work and bytes make
+    the reported figures."""
     import torch
     small = ("t", "g_oovv", "g_oooo", "g_ovvo")
     host = {k: T[k].cpu().pin_memory() for k in small + ("g_vvvv",)}
@@ -476,15 +489,19 @@ def run_e2e(eg, T, precision, args, o, v, step_flops, chunks=8, return_outputs=F
     for i in range(max(1, args.warmup if precision != "fp64" else 1)):
         step(i)
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s_in)
     for i in range(steps):
         step(i)
     e1.record(s_out)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    res = {"value": step_flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "ms_per_step": ms, "steps": steps,
+    if world > 1:
+        torch.distributed.barrier()
+    ms = reduce_max_ms(e0.elapsed_time(e1) / steps, world, "cuda")
+    res = {"value": job_tflops(step_flops, ms, world), "unit": "TFLOP/s", "h2d_bytes_per_step": world * h2d,
+           "d2h_bytes_per_step": world * d2h, "ms_per_step": ms, "steps": steps,
            "pipelining": f"uploads, contractions and read-backs on three streams; three sets of the 0.6 GB inputs; "
                          f"Wabef in {chunks} slabs of rows a through four slab buffers"}
     if return_outputs:
