@@ -71,6 +71,40 @@ __host__ __device__ inline void group_offsets32(const ModeGroup &g, uint32_t i, 
     }
 }
 
+// Compensated sum of one value pair (s, c) per thread over a block of NT
+// threads (NT a multiple of 32, at most 1024), in a fixed tree order: pairs are
+// merged with Knuth's TwoSum, the rounding error of each merge going to c.  The
+// depth is log2(NT) dependent merges, so the FP64 latency stays small (a serial
+// loop over the threads' sums would take NT of them).  Returns s + c in thread 0.
+template <int NT>
+__device__ __forceinline__ double block_sum_compensated(double s, double c, double *sh_s, double *sh_c) {
+    auto merge = [](double &a, double &ca, double b, double cb) {
+        const double t = a + b, bb = t - a;
+        const double e = (a - (t - bb)) + (b - bb);
+        a = t;
+        ca = (ca + cb) + e;
+    };
+    for (int o = 16; o > 0; o >>= 1) {
+        const double s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
+        merge(s, c, s2, c2);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        sh_s[w] = s;
+        sh_c[w] = c;
+    }
+    __syncthreads();
+    if (w == 0) {
+        s = lane < NT / 32 ? sh_s[lane] : 0.0;
+        c = lane < NT / 32 ? sh_c[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double s2 = __shfl_down_sync(0xffffffffu, s, o), c2 = __shfl_down_sync(0xffffffffu, c, o);
+            merge(s, c, s2, c2);
+        }
+    }
+    return s + c;
+}
+
 // Canonical contraction:  C[b,m,n] = cp*C + ab * sum_k A[b,m,k] B[b,n,k]
 //   batch: modes in A, B and C      m: modes in A and C (and C-only modes)
 //   n:     modes in B and C         k: summed modes (links; free modes under

@@ -108,10 +108,11 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_partial(ModeGroup k, const 
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
-// Sums the per-block partials in a fixed order with Neumaier compensation.
+// Sums the per-block partials in a fixed order: Neumaier compensation within a
+// thread, then a compensated tree across the block.
 __global__ void __launch_bounds__(kDotThreads) k_dot_final(const double *partial, int nparts, double *C, double cp,
                                                            double ab, bool zero) {
-    __shared__ double hi[kDotThreads], lo[kDotThreads];
+    __shared__ double sh_s[kDotThreads / 32], sh_c[kDotThreads / 32];
     double s = 0.0, c = 0.0;
     for (int i = threadIdx.x; i < nparts; i += kDotThreads) {
         const double x = partial[i];
@@ -119,20 +120,8 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_final(const double *partial
         c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
         s = t;
     }
-    hi[threadIdx.x] = s;
-    lo[threadIdx.x] = c;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double S = 0.0, Cc = 0.0;
-        for (int i = 0; i < kDotThreads; i++) {
-            const double x = hi[i];
-            const double t = S + x;
-            Cc += (fabs(S) >= fabs(x)) ? (S - t) + x : (x - t) + S;
-            S = t;
-            Cc += lo[i];
-        }
-        *C = epilogue(S + Cc, C, cp, ab, zero);
-    }
+    const double sum = block_sum_compensated<kDotThreads>(s, c, sh_s, sh_c);
+    if (threadIdx.x == 0) *C = epilogue(sum, C, cp, ab, zero);
 }
 
 // ------------------------------------------------------------------- gemv --

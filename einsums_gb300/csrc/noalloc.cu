@@ -79,11 +79,12 @@ __global__ void __launch_bounds__(kNoAllocThreads) k_dot_noalloc_partial(const d
     }
 }
 
-// One block: sums the partials in a fixed order (Neumaier-compensated), then
+// One block: sums the partials in a fixed order (Neumaier within a thread, a
+// compensated tree across the block), then
 // C = C_prefactor * C + AB_prefactor * sum, as the reference's DOT choice does.
 __global__ void __launch_bounds__(kNoAllocThreads) k_dot_noalloc_final(const double *partial, int nparts, double *C,
                                                                        double cp, double ab) {
-    __shared__ double hi[kNoAllocThreads], lo[kNoAllocThreads];
+    __shared__ double sh_s[kNoAllocThreads / 32], sh_c[kNoAllocThreads / 32];
     double s = 0.0, c = 0.0;
     for (int i = threadIdx.x; i < nparts; i += kNoAllocThreads) {
         const double x = partial[i];
@@ -91,20 +92,8 @@ __global__ void __launch_bounds__(kNoAllocThreads) k_dot_noalloc_final(const dou
         c += (fabs(s) >= fabs(x)) ? (s - t) + x : (x - t) + s;
         s = t;
     }
-    hi[threadIdx.x] = s;
-    lo[threadIdx.x] = c;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double S = 0.0, Cc = 0.0;
-        for (int i = 0; i < kNoAllocThreads; i++) {
-            const double x = hi[i];
-            const double t = S + x;
-            Cc += (fabs(S) >= fabs(x)) ? (S - t) + x : (x - t) + S;
-            S = t;
-            Cc += lo[i];
-        }
-        *C = cp * (*C) + ab * (S + Cc);
-    }
+    const double sum = block_sum_compensated<kNoAllocThreads>(s, c, sh_s, sh_c);
+    if (threadIdx.x == 0) *C = cp * (*C) + ab * sum;
 }
 
 } // namespace
