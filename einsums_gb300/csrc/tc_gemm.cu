@@ -456,6 +456,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         uint32_t aphase = 0;
         bool ok = true;
         const bool plain_store = p.zero && p.cp == 0.0;
+        const bool cp_one = p.cp == 1.0; // both tests once here: FP64 compares run on the slow FP64 pipe
         // The previous ("pending") tile: its int64 sums wait in this CTA's scratch
         // (column-major, so the warp's stores and loads of it are contiguous) and
         // are finished kFinCols columns at a time after each flush of the next
@@ -498,7 +499,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 v = int64_times_pow2(R, pend_rowExp + ce + p.shift_const);
                             if (!p.ab_pow2) v *= p.ab;
                             pend_C[rowOff + colOff[c0 + i]] =
-                                plain_store ? v : (p.cp == 1.0 ? old[i] + v : fma(p.cp, old[i], v));
+                                plain_store ? v : (cp_one ? old[i] + v : fma(p.cp, old[i], v));
                         }
                     }
                 }
@@ -535,7 +536,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         if (rowOkW[r] && colExp[c0 + c] != INT_MAX) {
                             const double v = finT[c * FIN_T + r];
                             pend_C[rowOffW[r] + colOff[c0 + c]] =
-                                plain_store ? v : (p.cp == 1.0 ? old[k] + v : fma(p.cp, old[k], v));
+                                plain_store ? v : (cp_one ? old[k] + v : fma(p.cp, old[k], v));
                         }
                     }
                     __syncwarp();
