@@ -456,14 +456,23 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     for (int64_t kb0 = 0; kb0 < nkb_total || kb0 == 0; kb0 += kb_per_pass) {
         p.kb0 = (int)kb0;
         p.nkb = (int)std::min<int64_t>(kb_per_pass, nkb_total - kb0);
-        // slices of at least 16 K blocks (one exact chunk), about one work entry per SM
+        // slices of at least 16 K blocks (one exact chunk); the count minimises the
+        // estimated makespan: rounds of work entries over the SMs times the K blocks
+        // of one entry, plus about four blocks' worth of per-entry epilogue work
         p.ksplit = 1;
         p.kslice = p.nkb;
         if (kslicing && p.nkb >= 32) {
-            const int want = (int)std::min<int64_t>(num_sms() / tiles, p.nkb / 16);
-            if (want > 1) {
-                p.kslice = (int)round_up((p.nkb + want - 1) / want, kKStep / kBK);
-                p.ksplit = (p.nkb + p.kslice - 1) / p.kslice;
+            int64_t best = -1;
+            for (int ks = 1; ks <= p.nkb / 16; ks++) {
+                const int64_t slice = round_up((p.nkb + ks - 1) / ks, kKStep / kBK);
+                const int64_t n = (p.nkb + slice - 1) / slice; // slices actually used
+                const int64_t rounds = (tiles * n + num_sms() - 1) / num_sms();
+                const int64_t cost = rounds * (slice + 4);
+                if (best < 0 || cost < best) {
+                    best = cost;
+                    p.kslice = (int)slice;
+                    p.ksplit = (int)n;
+                }
             }
         }
         if (p.ksplit > 1) {
