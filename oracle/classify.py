@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  This module is part of the CPU oracle: only the
 tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may
-import it, and only as the checker.  The product path classifies patterns in
+import it, and only to check results.  The product path classifies patterns in
 ``include/einsums_gb300/classify.hpp`` (compiled into the CUDA library) and
 never calls into ``oracle/``.
 

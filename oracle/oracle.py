@@ -1,8 +1,8 @@
 """CPU oracle for the einsum / permute hot path.
 
 TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and
-the CPU-baseline leg of ``bench.py`` may import this module, and only as the
-checker (or, in ``bench.py --impl reference``, as the timed CPU reference).
+the CPU-baseline leg of ``bench.py`` may import this module, and only to check
+results (or, in ``bench.py --impl reference``, as the timed CPU reference).
 The product path never routes through it.
 
 What it restates (reference paths relative to the Einsums project root):

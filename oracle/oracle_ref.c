@@ -2,8 +2,8 @@
  * CPU oracle: C restatement of the reference's scalar einsum loops.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py may load this library, and only as the
- * checker.  The product (einsums_gb300/) never links or calls it.
+ * CPU-baseline leg of bench.py may load this library, and only to check
+ * results.  The product (einsums_gb300/) never links or calls it.
  *
  * Functions here follow, loop for loop:
  *   oracle_generic_cpp  -- einsum_generic_algorithm / einsums_generic_target_loop /
