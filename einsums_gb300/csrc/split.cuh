@@ -92,24 +92,17 @@ __device__ __forceinline__ unsigned long long abs_bits(double x) {
 __device__ __forceinline__ long long scaled_round(double x, int sh) {
     const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
     const int ex = (int)((bits >> 52) & 0x7ff);
-    unsigned long long mant = bits & 0xFFFFFFFFFFFFFull;
-    int e2; // |x| 2^sh = mant * 2^e2
-    if (ex == 0) {
-        e2 = 1 - 1075 + sh;
-    } else {
-        mant |= 1ull << 52;
-        e2 = ex - 1075 + sh;
-    }
+    const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | ((unsigned long long)(ex != 0) << 52);
+    const int r = 1075 - (ex != 0 ? ex : 1) - sh; // |x| 2^sh = mant 2^-r
     unsigned long long q;
-    if (e2 >= 0) {
-        q = mant << (e2 < 11 ? e2 : 11); // not reached while |x| 2^sh < 2^52
-    } else if (e2 < -53) {
+    if (r <= 0) {
+        q = mant << (-r < 11 ? -r : 11); // not reached while |x| 2^sh < 2^52
+    } else if (r > 62) {
         q = 0; // below 1/2
     } else {
-        const int r = -e2; // 1..53
-        q = mant >> r;
-        const unsigned long long rem = mant & ((1ull << r) - 1), half = 1ull << (r - 1);
-        if (rem > half || (rem == half && (q & 1ull))) q++;
+        // round half to even in one add: the carry out of the r low bits happens
+        // exactly when they exceed half, or equal half with an odd quotient
+        q = (mant + ((1ull << (r - 1)) - 1ull) + ((mant >> r) & 1ull)) >> r;
     }
     return (bits >> 63) ? -(long long)q : (long long)q;
 }
@@ -145,12 +138,15 @@ __device__ __forceinline__ void digits_bf16x2(double x0, double x1, int e, uint3
     }();
     const int sh = kTopBits + kBits * (S - 1) - e;
     const long long G0 = scaled_round(x0, sh) + bias, G1 = scaled_round(x1, sh) + bias;
+    const uint32_t g0[2] = {(uint32_t)G0, (uint32_t)((unsigned long long)G0 >> 32)};
+    const uint32_t g1[2] = {(uint32_t)G1, (uint32_t)((unsigned long long)G1 >> 32)};
 #pragma unroll
     for (int s = 1; s < S; s++) {
-        const int p = 8 * (S - 1 - s);
-        const uint32_t u0 = (uint32_t)(G0 >> p) & 255u, u1 = (uint32_t)(G1 >> p) & 255u;
-        const float f0 = __uint_as_float(0x4B000000u | u0) - 8388735.0f;
-        const float f1 = __uint_as_float(0x4B000000u | u1) - 8388735.0f;
+        // byte S-1-s of G next to the bytes 00 00 4B: the float 2^23 + u in one permute
+        const int byte = S - 1 - s, w = byte >> 2;
+        const uint32_t sel = 0x7440u | (uint32_t)(byte & 3);
+        const float f0 = __uint_as_float(__byte_perm(g0[w], 0x4B000000u, sel)) - 8388735.0f;
+        const float f1 = __uint_as_float(__byte_perm(g1[w], 0x4B000000u, sel)) - 8388735.0f;
         out[s] = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
     }
     const int t0 = (int)(G0 >> (8 * (S - 1))), t1 = (int)(G1 >> (8 * (S - 1)));
