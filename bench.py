@@ -222,6 +222,22 @@ def host_cores():
         return os.cpu_count() or 1
 
 
+def host_cpu():
+    """The host CPU the baseline ran on: architecture, model (or the Arm implementer/part ids), cores usable."""
+    import platform
+    info = {"machine": platform.machine(), "cores_usable": host_cores(), "cores_online": os.cpu_count()}
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key, _, val = line.partition(":")
+                key, val = key.strip(), val.strip()
+                if key in ("model name", "CPU implementer", "CPU part") and key not in info:
+                    info[key] = val
+    except OSError:
+        pass
+    return info
+
+
 def reduce_max_ms(ms, world, device):
     """Max over ranks of a per-rank time: the job is as slow as its slowest rank."""
     if world == 1:
@@ -378,7 +394,7 @@ def run_ours(args, rank, world):
     if rank == 0 and world == 1 and not args.no_cpu:
         dt, fl, desc = cpu_sample(o, v, seed=args.seed)
         cpu = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": host_cores(), "kind": "port", "sample": desc,
-               "seconds": dt}
+               "seconds": dt, "cpu": host_cpu()}
 
     if rank == 0:
         line = {
@@ -528,7 +544,8 @@ def run_reference(args, rank, world):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (numpy PCG64, seeded)",
         "config": {"workload": f"CCD W intermediates o={o} v={v}: Wmnij, Wabef (GEMM), Wmbej (GENERIC), E (DOT)",
                    "precision": "fp64 (reference CPU einsum restated: OpenBLAS dgemm + OpenMP generic loop)"},
-        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": host_cores(), "kind": "port", "sample": desc},
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": host_cores(), "kind": "port", "sample": desc,
+                         "cpu": host_cpu()},
         "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
