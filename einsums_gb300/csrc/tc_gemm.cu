@@ -46,6 +46,7 @@ constexpr int THREADS = 320; // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int AUX_BYTES = 256;
 constexpr int kFinCols = 4;  // columns of the pending tile finished per batch
+constexpr int kDirectKB = 8; // tiles of at most this many K blocks are finished at their end, from TMEM
 constexpr int FIN_T = 33;    // padded row count of a warp's transposition buffer
 // per epilogue warp: 64 column offsets and exponents, the transposition buffer
 // of one batch, and its 32 rows' output offsets and validity
@@ -638,11 +639,14 @@ __global__ void __launch_bounds__(THREADS, 1)
                 group_offsets32(*job.mg, (uint32_t)m, oa, ob, rowOff);
                 rowExp = job.eA[m];
             }
+            // Short-K tiles (few chunks: the deferred finishing would run longer than
+            // the next tile's MMAs) are finished here, straight from TMEM.
+            const bool direct = p.ksplit == 1 && nkb <= kDirectKB;
             // K slices add their sums into the tile's accumulator; only the last
             // one to arrive at this warp's region finishes it
             long long *const dst = p.ksplit > 1 ? p.racc + (size_t)job.tid * kBM * kBN : rbc;
 #pragma unroll 1
-            for (int cc = 0; cc < kBN / 32; cc++) {
+            for (int cc = 0; cc < kBN / 32 && !direct; cc++) {
                 const uint32_t col = (uint32_t)(col0 + cc * 16);
                 uint32_t lo[16], hi[16];
                 ptx::tmem_ld16(tl + 256u + col, lo);
@@ -683,6 +687,64 @@ __global__ void __launch_bounds__(THREADS, 1)
             rowOffW[lane] = rowOff;
             rowOkW[lane] = row_ok ? 1 : 0;
             __syncwarp();
+            if (direct) {
+                // the same conversion and stores as finalize_cols, the sums read from TMEM
+                const bool rows_fast = job.mg->n > 0 && job.mg->s[2][job.mg->n - 1] == 1;
+                double *const Cj = job.C;
+#pragma unroll 1
+                for (int cc = 0; cc < kBN / 32; cc++) {
+                    uint32_t lo[16], hi[16];
+                    ptx::tmem_ld16(tl + 256u + (uint32_t)(col0 + cc * 16), lo);
+                    ptx::tmem_ld16(tl + 384u + (uint32_t)(col0 + cc * 16), hi);
+                    ptx::tmem_wait_ld();
+#pragma unroll
+                    for (int b = 0; b < 16; b += kFinCols) {
+                        const int c0 = cc * 16 + b;
+                        double v[kFinCols];
+#pragma unroll
+                        for (int i = 0; i < kFinCols; i++) {
+                            const int ce = colExp[c0 + i];
+                            v[i] = 0.0;
+                            if (row_ok && ce != INT_MAX) {
+                                long long R = (long long)(((unsigned long long)hi[b + i] << 32) | lo[b + i]);
+                                if (p.ab_neg) R = -R;
+                                if (rowExp == INT_MIN || ce == INT_MIN)
+                                    v[i] = __longlong_as_double(0x7ff8000000000000ll);
+                                else
+                                    v[i] = int64_times_pow2(R, rowExp + ce + p.shift_const);
+                                if (!p.ab_pow2) v[i] *= p.ab;
+                            }
+                        }
+                        if (rows_fast) {
+                            if (row_ok) {
+#pragma unroll
+                                for (int i = 0; i < kFinCols; i++) {
+                                    if (colExp[c0 + i] == INT_MAX) continue;
+                                    double *const cp_ = Cj + rowOff + colOff[c0 + i];
+                                    *cp_ = plain_store ? v[i] : (cp_one ? *cp_ + v[i] : fma(p.cp, *cp_, v[i]));
+                                }
+                            }
+                        } else {
+#pragma unroll
+                            for (int i = 0; i < kFinCols; i++) finT[i * FIN_T + lane] = v[i];
+                            __syncwarp();
+                            // lanes 4r..4r+3 take the batch's columns of row r (8 rows per pass)
+#pragma unroll
+                            for (int k = 0; k < kFinCols; k++) {
+                                const int e = k * 32 + lane, r = e / kFinCols, c = e % kFinCols;
+                                if (rowOkW[r] && colExp[c0 + c] != INT_MAX) {
+                                    const double w = finT[c * FIN_T + r];
+                                    double *const cp_ = Cj + rowOffW[r] + colOff[c0 + c];
+                                    *cp_ = plain_store ? w : (cp_one ? *cp_ + w : fma(p.cp, *cp_, w));
+                                }
+                            }
+                            __syncwarp();
+                        }
+                    }
+                }
+                ptx::tc_fence_before();
+                finish = false; // nothing left pending
+            }
             pend = finish;
             pend_src = dst;
             pend_done = 0;
