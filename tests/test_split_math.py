@@ -1,9 +1,11 @@
 """CPU check of the split-BF16 arithmetic used by the GPU kernels: row
 exponents, balanced base-256 digits (each exact in BF16), triangular
 truncation of the digit products, and exact integer accumulation.  A numpy
-restatement of einsums_gb300/csrc/split.cu:to_digits and the epilogue's
+restatement of einsums_gb300/csrc/split.cuh:to_digits and the epilogue's
 R = sum_d 2^(8(S-1-d)) G_d; checks the reconstruction and the stated error
-bound, and the FP32-exactness limits the kernel relies on."""
+bound, and the FP32-exactness limits the kernel relies on.  A bit-level
+restatement of the device's scaled_round / digits_bf16x2 (one add-and-shift
+rounding, bias, byte permute, FP32 add) is checked against the definition."""
 import math
 
 import numpy as np
@@ -92,3 +94,64 @@ def test_int64_accumulator_limit():
         kmax = int(2 ** 62 / (2 ** 14 * w)) // 64 * 64
         assert kmax * 2 ** 14 * w <= 2 ** 62
         assert kmax >= 64
+
+
+# ---- bit-level restatement of the device digit arithmetic (split.cuh) ------
+def _scaled_round_dev(x, sh):
+    """scaled_round: round(x 2^sh) half to even in one add-and-shift on the IEEE fields."""
+    import struct
+    bits = struct.unpack("<Q", struct.pack("<d", x))[0]
+    ex = (bits >> 52) & 0x7FF
+    mant = (bits & 0xFFFFFFFFFFFFF) | ((1 if ex else 0) << 52)
+    r = 1075 - (ex if ex else 1) - sh
+    if r <= 0:
+        q = (mant << min(-r, 11)) & (2 ** 64 - 1)
+    elif r > 62:
+        q = 0
+    else:
+        q = ((mant + ((1 << (r - 1)) - 1) + ((mant >> r) & 1)) & (2 ** 64 - 1)) >> r
+    return -q if bits >> 63 else q
+
+
+def _byte_perm(x, y, s):
+    b = [(x >> (8 * i)) & 255 for i in range(4)] + [(y >> (8 * i)) & 255 for i in range(4)]
+    return sum(b[(s >> (4 * i)) & 7] << (8 * i) for i in range(4))
+
+
+def _f32(u):
+    import struct
+    return np.float32(struct.unpack("<f", struct.pack("<I", u & 0xFFFFFFFF))[0])
+
+
+def _digits_dev(x, e, S):
+    """digits_bf16x2 for one value: bias, byte permute to 2^23 + u, one FP32 add per digit."""
+    bias = 0
+    for _ in range(1, S):
+        bias = bias * 256 + 127
+    G = _scaled_round_dev(x, TOP + BITS * (S - 1) - e) + bias
+    Gu = G & (2 ** 64 - 1)
+    words = [Gu & 0xFFFFFFFF, Gu >> 32]
+    out = [0] * S
+    for s in range(1, S):
+        byte = S - 1 - s
+        f = _f32(_byte_perm(words[byte >> 2], 0x4B000000, 0x7440 | (byte & 3))) - np.float32(8388735.0)
+        assert float(f).is_integer()
+        out[s] = int(f)
+    f0 = _f32(0x4B400000 + (G >> (8 * (S - 1)))) - np.float32(12582912.0)
+    out[0] = int(f0)
+    return out
+
+
+@pytest.mark.parametrize("S", [2, 3, 4, 5, 6])
+def test_device_digit_arithmetic_matches_the_definition(S):
+    rng = np.random.default_rng(40 + S)
+    X = rng.standard_normal((12, 24)) * np.exp2(rng.integers(-30, 30, size=(12, 1)))
+    X[0, :5] = [0.0, -0.0, 5e-324, -1e-310, 1.0]
+    X[1, :] = np.ldexp(np.round(rng.standard_normal(24) * 2 ** 20) + 0.5, -20)  # exact ties
+    e = exponents(X)
+    D = digits(X, e, S)
+    for i in range(X.shape[0]):
+        sh = TOP + BITS * (S - 1) - int(e[i])
+        for j in range(X.shape[1]):
+            assert _scaled_round_dev(float(X[i, j]), sh) == int(np.rint(np.ldexp(X[i, j], sh)))
+            assert _digits_dev(float(X[i, j]), int(e[i]), S) == [int(D[s, i, j]) for s in range(S)]
