@@ -70,6 +70,8 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    INTERVAL_MS = 50
+
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
@@ -78,10 +80,14 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi takes a while to print its first line: start the work only once it samples
+            t0 = time.time()
+            while not self.lines and self.proc.poll() is None and time.time() - t0 < 3.0:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
