@@ -155,3 +155,42 @@ def test_device_digit_arithmetic_matches_the_definition(S):
         for j in range(X.shape[1]):
             assert _scaled_round_dev(float(X[i, j]), sh) == int(np.rint(np.ldexp(X[i, j], sh)))
             assert _digits_dev(float(X[i, j]), int(e[i]), S) == [int(D[s, i, j]) for s in range(S)]
+
+
+def _int64_times_pow2_dev(R, e):
+    """int64_times_pow2 of the tensor kernel's epilogue: R * 2^e rounded to nearest
+    even, built on the IEEE fields (leading-zero count, 53-bit mantissa with
+    half-even rounding of the 11 dropped bits); None where the kernel leaves the
+    result to its FP64 fallback (exponent out of the normal range)."""
+    if R == 0:
+        return 0.0
+    a = -R if R < 0 else R
+    lz = 64 - a.bit_length()
+    x = (a << lz) & (2 ** 64 - 1)
+    mant, rem = x >> 11, x & 0x7FF
+    if rem > 0x400 or (rem == 0x400 and (mant & 1)):
+        mant += 1
+    exp = 63 - lz + e
+    if mant >> 53:
+        mant >>= 1
+        exp += 1
+    biased = exp + 1023
+    if biased <= 0 or biased >= 2047:
+        return None
+    import struct
+    bits = ((1 << 63) if R < 0 else 0) | (biased << 52) | (mant & 0xFFFFFFFFFFFFF)
+    return struct.unpack("<d", struct.pack("<Q", bits))[0]
+
+
+def test_epilogue_int64_to_double_rounds_half_even():
+    rng = np.random.default_rng(77)
+    cases = [1, -1, 2 ** 53 - 1, 2 ** 53, 2 ** 53 + 1, 2 ** 53 + 3, -(2 ** 54 + 2), 2 ** 62 + 2 ** 9,
+             2 ** 62 + 2 ** 10, 2 ** 62 + 3 * 2 ** 9, 2 ** 63 - 1, -(2 ** 63 - 1), (2 ** 53 - 1) << 10]
+    cases += [int(v) for v in rng.integers(-2 ** 62, 2 ** 62, size=400)]
+    cases += [int(v) << int(s) for v, s in zip(rng.integers(-2 ** 20, 2 ** 20, size=100), rng.integers(0, 40, size=100))]
+    for R in cases:
+        for e in (-1074 + 64, -200, -46, 0, 17, 900):
+            got = _int64_times_pow2_dev(R, e)
+            if got is None:
+                continue  # out of the normal range: the kernel's FP64 fallback handles it
+            assert got == math.ldexp(float(R), e), (R, e)  # float(int) rounds half to even
