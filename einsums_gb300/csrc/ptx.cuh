@@ -75,29 +75,6 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const void *tmap, uint64_
         : "memory");
 }
 
-// 3-D tiled load multicast to every CTA of the cluster in `mask`: the box lands
-// at the same shared-memory offset in each, completing on each one's `bar`.
-__device__ __forceinline__ void tma_load_3d_mc(void *dst, const void *tmap, uint64_t *bar, int c0, int c1, int c2,
-                                               uint16_t mask) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-        " [%0], [%1, {%3, %4, %5}], [%2], %6;" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "h"(mask)
-        : "memory");
-}
-
-// ----------------------------------------------------------------- cluster --
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-
-// Whole-cluster barrier (every thread of every CTA of the cluster).
-__device__ __forceinline__ void cluster_sync() {
-    asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
 // ---------------------------------------------------------------- tcgen05 --
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
@@ -130,15 +107,6 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint6
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
-}
-
-// As mma_commit, arriving on `bar` in every CTA of the cluster in `mask`.
-__device__ __forceinline__ void mma_commit_mc(uint64_t *bar, uint16_t mask) {
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-            smem_u32(bar)),
-        "h"(mask)
-        : "memory");
 }
 
 // Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.

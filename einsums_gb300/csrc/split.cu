@@ -261,14 +261,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 3-D map over [planes][rows][Kp] BF16, box 64 (k) x box_rows x 1, 128-byte swizzle.
-eg_status encode_planes(CUtensorMap *map, void *base, int64_t Kp, int64_t rows, int64_t planes,
-                        int box_rows = kBM) {
+// 3-D map over [planes][rows][Kp] BF16, box 64 (k) x 128 rows x 1, 128-byte swizzle.
+eg_status encode_planes(CUtensorMap *map, void *base, int64_t Kp, int64_t rows, int64_t planes) {
     auto fn = encode_fn();
     if (!fn) return fail(EG_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
     cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)planes};
     cuuint64_t strides[2] = {(cuuint64_t)(Kp * 2), (cuuint64_t)(Kp * 2 * rows)};
-    cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)box_rows, 1};
+    cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)kBM, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -372,8 +371,7 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     const int64_t nb = c.batch.total, M = c.m.total, N = c.n.total, K = c.k.total;
     if (M >= (int64_t(1) << 31) || N >= (int64_t(1) << 31) || K >= (int64_t(1) << 31) || nb * S >= (int64_t(1) << 31))
         return fail(EG_ERROR_NOT_SUPPORTED, "split form: a mode group exceeds 2^31 elements");
-    // rows of A padded to whole pairs of tiles, so cluster pairs never run past the planes
-    const int64_t Kp = round_up(K, kKStep), Mp = round_up(M, 2 * kBM), Np = round_up(N, kBN);
+    const int64_t Kp = round_up(K, kKStep), Mp = round_up(M, kBM), Np = round_up(N, kBN);
 
     // workspace: digit planes of A and B, row maxima, exponents, status word
     const size_t bytesA = (size_t)nb * S * Mp * Kp * 2, bytesB = (size_t)nb * S * Np * Kp * 2;
@@ -413,10 +411,9 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
                             tables ? tab + M + K + N : nullptr)) != EG_SUCCESS)
         return st;
 
-    CUtensorMap tmA, tmB, tmBh;
+    CUtensorMap tmA, tmB;
     if ((st = encode_planes(&tmA, planesA, Kp, Mp, nb * S)) != EG_SUCCESS) return st;
     if ((st = encode_planes(&tmB, planesB, Kp, Np, nb * S)) != EG_SUCCESS) return st;
-    if ((st = encode_planes(&tmBh, planesB, Kp, Np, nb * S, kBN / 2)) != EG_SUCCESS) return st;
 
     TcGemmParams p{};
     p.S = S;
@@ -490,7 +487,7 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
             EG_CUDA(cudaMemsetAsync(prof, 0, (size_t)num_sms() * 8 * sizeof(unsigned long long), s));
         }
         p.prof = prof;
-        if ((st = launch_tc_gemm(tmA, tmB, tmBh, p, s)) != EG_SUCCESS) return st;
+        if ((st = launch_tc_gemm(tmA, tmB, p, s)) != EG_SUCCESS) return st;
         if (prof) {
             // Per-role wait/busy cycles summed over CTAs (a tracing aid, off by default).
             std::vector<unsigned long long> h((size_t)num_sms() * 8);

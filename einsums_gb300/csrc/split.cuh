@@ -157,10 +157,7 @@ __device__ __forceinline__ void digits_bf16x2(double x0, double x1, int e, uint3
 
 // Sets the kernels' shared-memory attribute once (call outside stream capture).
 eg_status ensure_tc_attributes();
-// tmBh: the B planes with a 64-row box (half a tile), used when two CTAs of a
-// cluster multicast the halves of a shared B tile (mtiles even).
-eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const CUtensorMap &tmBh,
-                         const TcGemmParams &p, cudaStream_t s);
+eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p, cudaStream_t s);
 // Grouped form: `ntiles_total` work entries, per-tile parameters from `items`.
 eg_status launch_tc_gemm_grouped(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p,
                                  const TcItem *items, const int4 *work, int ntiles_total, cudaStream_t s);

@@ -90,26 +90,15 @@ struct TileJob {
     double *C;          // output base of this (item, batch)
 };
 
-// Tile t of the schedule.  With CL = 2 the schedule runs over pairs of row
-// tiles (the cluster's two CTAs take rows 2*mp and 2*mp + 1 of one column of
-// tiles and share its B tile).
-template <bool GROUPED, int CL>
-__device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *items, const int4 *work, int t,
-                                           uint32_t crank) {
+// Tile t of the schedule.
+template <bool GROUPED>
+__device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *items, const int4 *work, int t) {
     TileJob j;
     if (!GROUPED) {
         int b;
         const int ks = t % p.ksplit;
         t /= p.ksplit;
-        if (CL == 1) {
-            tile_coords(p, t, b, j.mt, j.nt);
-        } else {
-            TcGemmParams q = p;
-            q.mtiles = p.mtiles / CL;
-            int mp;
-            tile_coords(q, t, b, mp, j.nt);
-            j.mt = mp * CL + (int)crank;
-        }
+        tile_coords(p, t, b, j.mt, j.nt);
         j.zA = b * p.S;
         j.zB = b * p.S;
         j.kbeg = ks * p.kslice;
@@ -247,11 +236,11 @@ __device__ __forceinline__ void raise_abort(const TcGemmParams &p, volatile int 
 
 // 10 warps: two of the four SM sub-partitions hold three warps, so the
 // 16K-register file of a sub-partition caps a thread at 168 registers.
-template <bool GROUPED, int CL>
+template <bool GROUPED>
 __global__ void __launch_bounds__(THREADS, 1)
     k_tc_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                    const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ TcGemmParams p,
-                    const TcItem *items, const int4 *work, int ntiles_total) {
+                    const __grid_constant__ TcGemmParams p, const TcItem *items, const int4 *work,
+                    int ntiles_total) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
@@ -274,7 +263,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (threadIdx.x == 0) {
         for (int i = 0; i < STAGES; i++) {
             ptx::mbar_init(&full[i], 1);
-            ptx::mbar_init(&empty[i], CL); // every CTA of the cluster consumes each stage
+            ptx::mbar_init(&empty[i], 1);
         }
         for (int i = 0; i < 2; i++) {
             ptx::mbar_init(&accf[i], 1);
@@ -292,13 +281,9 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncthreads();
     ptx::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    // Peers multicast into this CTA's shared memory and arrive on its barriers:
-    // they must see the barriers initialised first.
-    if (CL > 1) ptx::cluster_sync();
-    const uint32_t crank = CL > 1 ? ptx::cluster_ctarank() : 0u;
-    const int cta0 = blockIdx.x / CL, ctas = gridDim.x / CL; // schedule index and stride of this cluster
+    const int cta0 = blockIdx.x, ctas = gridDim.x; // schedule index and stride of this CTA
 
-    const int total_tiles = GROUPED ? ntiles_total : p.nbatch * (p.mtiles / CL) * p.ntiles * p.ksplit;
+    const int total_tiles = GROUPED ? ntiles_total : p.nbatch * p.mtiles * p.ntiles * p.ksplit;
     const int S = p.S;
 
     if (warp == 0) {
@@ -311,7 +296,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             int issued = 0; // slots that have received a group (they fill in order 0, 1, 2)
             bool ok = true;
             for (int tile = cta0; tile < total_tiles && ok; tile += ctas) {
-                const TileJob job = resolve<GROUPED, CL>(p, items, work, tile, crank);
+                const TileJob job = resolve<GROUPED>(p, items, work, tile);
                 for (int d = 0; d < S && ok; d++) {
                     for (int s = 0; s <= d && ok; s++) {
                         const int t = d - s;
@@ -331,14 +316,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 const int kc = (p.kb0 + job.kbeg + kb + h) * kBK;
                                 ptx::tma_load_3d(sa + h * A_BYTES, &tmA, &full[stage], kc, job.mt * kBM, job.zA + s);
                                 uint8_t *sb = sa + GROUP_KB * A_BYTES + h * B_BYTES;
-                                if (CL == 1) {
-                                    ptx::tma_load_3d(sb, &tmB, &full[stage], kc, job.nt * kBN, job.zB + t);
-                                } else {
-                                    // this CTA's half of the shared B tile, written into both CTAs
-                                    ptx::tma_load_3d_mc(sb + crank * (B_BYTES / CL), &tmBh, &full[stage], kc,
-                                                        job.nt * kBN + (int)crank * (kBN / CL), job.zB + t,
-                                                        (uint16_t)((1u << CL) - 1));
-                                }
+                                ptx::tma_load_3d(sb, &tmB, &full[stage], kc, job.nt * kBN, job.zB + t);
                             }
                             if (issued < STAGES) issued++;
                             if (++stage == STAGES) {
@@ -410,10 +388,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                 const uint32_t nphase = ST == STAGES - 1 ? phase ^ 1 : phase;
                 ready = mma_group<2>(dt, da, db, idesc, in_chunk > 0 ? 1u : 0u,
                                      full_base + (uint32_t)(((ST + 1) % STAGES) * 8), nphase);
-                if (CL == 1)
-                    ptx::mma_commit(&empty[ST]);
-                else
-                    ptx::mma_commit_mc(&empty[ST], (uint16_t)((1u << CL) - 1));
+                ptx::mma_commit(&empty[ST]);
                 phase = nphase;
                 if (++in_chunk == kChunkKB / GROUP_KB) close_chunk();
                 if (++g == gpp) {
@@ -629,7 +604,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const long long tfin = (p.prof && ew == 0 && lane == 0) ? clock64() : 0;
             finalize_cols(kBN / 2);
             __syncwarp();
-            const TileJob job = resolve<GROUPED, CL>(p, items, work, tile, crank);
+            const TileJob job = resolve<GROUPED>(p, items, work, tile);
             const int64_t m = (int64_t)job.mt * kBM + row;
             const bool row_ok = m < job.M;
             int64_t rowOff = 0;
@@ -758,8 +733,6 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 
     __syncthreads();
-    // no CTA leaves while a peer may still write into its shared memory
-    if (CL > 1) ptx::cluster_sync();
     if (p.prof && threadIdx.x == 0) prof_add(p, kProfTotal, clock64() - t_start);
     if (warp == 1) {
         ptx::tc_fence_after();
@@ -773,51 +746,23 @@ eg_status ensure_tc_attributes() {
     static std::once_flag once;
     static cudaError_t err = cudaSuccess;
     std::call_once(once, [] {
-        err = cudaFuncSetAttribute(k_tc_split_gemm<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        err = cudaFuncSetAttribute(k_tc_split_gemm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (err == cudaSuccess)
-            err = cudaFuncSetAttribute(k_tc_split_gemm<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       SMEM_BYTES);
-        if (err == cudaSuccess)
-            err = cudaFuncSetAttribute(k_tc_split_gemm<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       SMEM_BYTES);
+            err = cudaFuncSetAttribute(k_tc_split_gemm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     });
     if (err != cudaSuccess) return cuda_fail(err, "cudaFuncSetAttribute(k_tc_split_gemm)");
     return EG_SUCCESS;
 }
 
-eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const CUtensorMap &tmBh,
-                         const TcGemmParams &p, cudaStream_t s) {
+eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p, cudaStream_t s) {
     eg_status st = ensure_tc_attributes();
     if (st != EG_SUCCESS) return st;
     const int total = p.nbatch * p.mtiles * p.ntiles * p.ksplit;
     if (total <= 0) return EG_SUCCESS;
-    if (p.mtiles % 2 == 0) {
-        // clusters of two CTAs on vertically adjacent tiles share B through multicast
-        const int pairs = total / 2;
-        const int clusters = pairs < num_sms() / 2 ? pairs : num_sms() / 2;
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3((unsigned)(clusters * 2));
-        cfg.blockDim = dim3(THREADS);
-        cfg.dynamicSmemBytes = SMEM_BYTES;
-        cfg.stream = s;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = 2;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        {
-            LaunchScope ls_("k_tc_split_gemm", s);
-            EG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_split_gemm<false, 2>, tmA, tmB, tmBh, p, (const TcItem *)nullptr,
-                                       (const int4 *)nullptr, 0));
-        }
-        return EG_SUCCESS;
-    }
     const int grid = total < num_sms() ? total : num_sms();
     {
         LaunchScope ls_("k_tc_split_gemm", s);
-        k_tc_split_gemm<false, 1><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, tmBh, p, nullptr, nullptr, 0);
+        k_tc_split_gemm<false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p, nullptr, nullptr, 0);
     }
     EG_CHECK_LAUNCH("k_tc_split_gemm");
     return EG_SUCCESS;
@@ -831,7 +776,7 @@ eg_status launch_tc_gemm_grouped(const CUtensorMap &tmA, const CUtensorMap &tmB,
     const int grid = ntiles_total < num_sms() ? ntiles_total : num_sms();
     {
         LaunchScope ls_("k_tc_split_gemm_grouped", s);
-        k_tc_split_gemm<true, 1><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, tmB, p, items, work, ntiles_total);
+        k_tc_split_gemm<true><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p, items, work, ntiles_total);
     }
     EG_CHECK_LAUNCH("k_tc_split_gemm_grouped");
     return EG_SUCCESS;
