@@ -17,11 +17,14 @@
 //    own partial before the final pass reads it, so nothing carries over
 //    between calls, but two calls whose kernels overlap on the GPU (different
 //    streams, or host threads) race on the array;
-//  * the first call on a device, with that device current, looks up the
-//    array's device address (cudaGetSymbolAddress); make that first call
-//    before any stream capture.
-#include <mutex>
-
+//  * every call looks up the array's device address on the current device
+//    (cudaGetSymbolAddress, which allocates nothing), so the address stays
+//    right after a device reset or a new primary context; the first call on a
+//    device also loads the library's device code there, so make that first
+//    call before any stream capture;
+//  * C is C_prefactor * C + AB_prefactor * sum, as the reference's C++ DOT
+//    choice computes it: with C_prefactor == 0 a NaN or infinity already in C
+//    stays in the result (eg_einsum with C++ semantics does the same).
 #include "common.cuh"
 
 namespace eg {
@@ -31,27 +34,17 @@ namespace {
 constexpr int kNoAllocParts = 4096;
 constexpr int64_t kNoAllocChunk = 65536;
 constexpr int kNoAllocThreads = 256;
-constexpr int kMaxDevices = 64;
 
 // The scratch: kNoAllocParts doubles (32 KB) on every device that loads the library.
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocParts];
 
-// Host-side view: the address of the array on each device, looked up once.
-double *g_scratch_ptr[kMaxDevices] = {};
-std::mutex g_scratch_mutex;
-
+// The array's address on the current device.  In host code the symbol
+// g_noalloc_partials is only a host-side stand-in, never a device address.
 eg_status scratch_on_current_device(double **out) {
-    int dev = 0;
-    EG_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return fail(EG_ERROR_NOT_SUPPORTED, "eg_dot_noalloc: device index too large");
-    std::lock_guard<std::mutex> lk(g_scratch_mutex);
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_partials);
-        if (err != cudaSuccess) return cuda_fail(err, "cudaGetSymbolAddress(g_noalloc_partials)");
-        g_scratch_ptr[dev] = (double *)p;
-    }
-    *out = g_scratch_ptr[dev];
+    void *p = nullptr;
+    cudaError_t err = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (err != cudaSuccess) return cuda_fail(err, "cudaGetSymbolAddress(g_noalloc_partials)");
+    *out = (double *)p;
     return EG_SUCCESS;
 }
 

@@ -142,8 +142,10 @@ eg_status eg_einsum_batched(double C_prefactor, const int32_t *C_labels, const e
  * latency-critical loops that must not pay for an allocation.  The partial sums live in a
  * fixed 32 KB array inside the library (4096 partials of 65536 elements each), so n is at
  * most 2^28; longer inputs return EG_ERROR_NOT_SUPPORTED.  Every call on a device shares that
- * array: calls whose kernels overlap on the GPU race.  The first call on a device, with that
- * device current, looks the array up (cudaGetSymbolAddress); make it before any stream capture.
+ * array: calls whose kernels overlap on the GPU race.  Each call looks the array up on the
+ * current device (cudaGetSymbolAddress); the first call on a device also loads the library's
+ * device code there, so make it before any stream capture.  As in the reference's C++ DOT
+ * choice, C is multiplied by C_prefactor even when that is 0, so a NaN in C survives.
  */
 eg_status eg_dot_noalloc(double C_prefactor, double *C, double AB_prefactor, const double *A, const double *B,
                          int64_t n, void *stream);
