@@ -191,33 +191,52 @@ def oracle_sample_check(T, W_fp64, o, v, rows=2):
     return out
 
 
-def cpu_sample(o, v, seed=0, frac_rows=None, threads=None):
-    """The oracle's CCD step on a bounded sample (slabs of the leading output
-    index); returns (seconds, algorithmic flops of the sample, description)."""
+def oracle_threads():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    return int(oracle.lib().oracle_num_threads())
+
+
+def cpu_sample(o, v, seed=0, cores=None, b_rows=None, a_rows=None):
+    """The oracle's CCD step on a bounded sample; returns (seconds, algorithmic
+    flops of the sample, description).
+
+    The reference's generic loop runs OpenMP over the outermost target index
+    only (Backends/BaseAlgebra.hpp:70-80), so the Wmnij and Wmbej slabs keep at
+    least as many rows of m as the host has cores (all of them on a box with
+    o or fewer cores): every core works, as it would on the whole step.
+    Wmbej may also be cut along b, Wabef (a dgemm, threaded by OpenBLAS) along
+    a; E is computed whole."""
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from einsums_gb300 import workloads
+    cores = cores or host_cores()
     T = workloads.ccd_inputs(o, v, seed=seed, backend="numpy", with_vvvv=False)
     t, g = T["t"], T["g_oovv"]
-    a_rows = frac_rows or max(1, v // 32)
-    m_rows = max(1, o // 16)
+    m_rows = min(o, max(1, cores))
+    b_rows = min(v, b_rows or v)
+    a_rows = min(v, a_rows or max(1, v // 32))
     W1 = np.zeros((m_rows, o, o, o))
     W2 = np.zeros((a_rows, v, v, v))
-    W3 = np.zeros((m_rows, v, v, o))
+    W3 = np.zeros((m_rows, b_rows, v, o))
     E = np.zeros(())
     g_m = np.ascontiguousarray(g[:m_rows])
     t_a = np.ascontiguousarray(t[:, :, :a_rows])
+    t_b = np.ascontiguousarray(t[:, :, :, :b_rows])
     t0 = time.perf_counter()
     oracle.einsum("mnij", W1, 1.0, 0.25, "ijef", t, "mnef", g_m)
     oracle.einsum("abef", W2, 1.0, 0.25, "mnef", g, "mnab", t_a)
-    oracle.einsum("mbej", W3, 1.0, -0.5, "jnfb", t, "mnef", g_m)
+    oracle.einsum("mbej", W3, 1.0, -0.5, "jnfb", t_b, "mnef", g_m)
     oracle.einsum("", E, 0.0, 0.25, "ijab", t, "ijab", g)
     dt = time.perf_counter() - t0
     f = flops(o, v)
-    fl = f["Wmnij"] * m_rows / o + f["Wabef"] * a_rows / v + f["Wmbej"] * m_rows / o + f["E"]
-    desc = (f"oracle CCD step on slabs: Wmnij/Wmbej rows m<{m_rows} of {o}, Wabef rows a<{a_rows} of {v}, "
-            f"full E; numpy OpenBLAS dgemm + OpenMP generic loop")
+    fl = f["Wmnij"] * m_rows / o + f["Wabef"] * a_rows / v + f["Wmbej"] * m_rows / o * b_rows / v + f["E"]
+    full = sum(f.values())
+    desc = (f"oracle CCD step on a sample of {100 * fl / full:.1f}% of the step's flops: Wmnij rows m<{m_rows} "
+            f"of {o} ({100 * m_rows / o:.0f}%), Wabef rows a<{a_rows} of {v} ({100 * a_rows / v:.1f}%), Wmbej rows "
+            f"m<{m_rows}, b<{b_rows} ({100 * m_rows * b_rows / (o * v):.1f}%), full E; numpy OpenBLAS dgemm + "
+            f"OpenMP generic loop over m on {oracle_threads()} threads")
     return dt, fl, desc
 
 
@@ -398,9 +417,21 @@ def run_ours(args, rank, world):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        dt, fl, desc = cpu_sample(o, v, seed=args.seed)
-        cpu = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": host_cores(), "kind": "port", "sample": desc,
-               "seconds": dt, "cpu": host_cpu()}
+        # three runs of the sample (10-30 s of CPU work on the GPU machine's host); the median rate
+        runs = [cpu_sample(o, v, seed=args.seed) for _ in range(3)]
+        dt = statistics.median(r[0] for r in runs)
+        fl, desc = runs[0][1], runs[0][2]
+        cpu = {"value": fl / dt / 1e12, "unit": "TFLOP/s", "cores": oracle_threads(), "kind": "port",
+               "sample": desc + "; median of 3 runs", "seconds": dt, "cpu": host_cpu()}
+
+    # The other configurations at their full sizes, after the timed region, with
+    # their oracle parity checks (rank 0 of a single-GPU run only).
+    suites = None
+    if rank == 0 and world == 1 and not args.no_suites:
+        del T, W64
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        suites = run_suites_inline(eg)
 
     if rank == 0:
         line = {
@@ -419,6 +450,7 @@ def run_ours(args, rank, world):
             "per_contraction_ms": per_contraction, "kernels": kernels, "kernels_steps": args.steps + args.warmup,
             "error_vs_fp64": errors, "error_fp64_vs_oracle_sample": oracle_err, "split_report": split_report,
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches,
+            "suites": suites,
         }
         print(json.dumps(line))
 
@@ -610,6 +642,21 @@ def suite_fock(eg, n=100):
     tK = time.perf_counter() - t0
     for prec in ("fp64", "split_bf16"):
         out[prec]["error_vs_oracle"] = oracle.rel_fro(out[prec].pop("F"), Fref)
+    # the whole F = 2 J - K: the two einsum calls against the symmetric-integral entry point
+    # (reads the canonical eighth of g; 0.75 n^4 FP64 multiply-adds against 2 n^4)
+    def two_calls():
+        eg.einsum(0.0, "pq", F, 2.0, "pqrs", g, "rs", D)
+        eg.einsum(1.0, "pq", F, -1.0, "prqs", g, "rs", D)
+    ms_two = _time(two_calls, reps=20, warm=3)
+    Fs = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    ms_sym = _time(lambda: eg.fock_jk_symmetric(Fs, g, D, F_prefactor=0.0), reps=20, warm=3)
+    pk, pk_kind = peaks()
+    out["F_2J_minus_K"] = {
+        "two_einsum_calls_ms": ms_two, "symmetric_entry_ms": ms_sym, "speedup": ms_two / ms_sym,
+        "symmetric_error_vs_oracle": oracle.rel_fro(Fs.cpu().numpy(), Fref),
+        "symmetric_fp64_fma": 0.75 * n ** 4, "symmetric_unique_bytes": 8.0 * n ** 4 / 8,
+        "symmetric_equiv_tflops": 4.0 * n ** 4 / ms_sym / 1e9,
+        "note": "equiv TFLOP/s counts the 4 n^4 flops of the two general contractions"}
     out["cpu_oracle"] = {"J_ms": tJ * 1e3, "K_ms": tK * 1e3, "cores": host_cores()}
     return out
 
@@ -656,7 +703,10 @@ def suite_permute(eg, sizes=(32, 64, 128, 256)):
 
 def suite_contraction(eg, sizes=(64, 128)):
     """Config 3b: C[i,k,j,l] = sum_mn A[i,m,j,n] B[m,k,n,l]; FP64 and split S = 3..6."""
+    import numpy as np
     import torch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
     from einsums_gb300 import workloads
     res = {"config": "generic contraction ikjl <- imjn * mknl", "sizes": {}}
     for n in sizes:
@@ -666,6 +716,13 @@ def suite_contraction(eg, sizes=(64, 128)):
         alg = eg.einsum(0.0, "ikjl", C64, 1.0, "imjn", A, "mknl", B)
         ms64 = _time(lambda: eg.einsum(0.0, "ikjl", C64, 1.0, "imjn", A, "mknl", B), reps=1, warm=0)
         entry = {"algorithm": alg, "fp64": {"ms": ms64, "tflops": flop / ms64 / 1e9}}
+        # the oracle on a slab of C (rows i < ri, k < rk): the reference's generic loop
+        ri, rk = (16, n) if n <= 64 else (1, 8)
+        ref = np.zeros((ri, rk, n, n))
+        oracle.einsum("ikjl", ref, 0.0, 1.0, "imjn", np.ascontiguousarray(A[:ri].cpu().numpy()), "mknl",
+                      np.ascontiguousarray(B[:, :rk].cpu().numpy()))
+        entry["fp64"]["error_vs_oracle_slab"] = oracle.rel_fro(C64[:ri, :rk].cpu().numpy(), ref)
+        entry["fp64"]["oracle_slab"] = f"i<{ri}, k<{rk}"
         C = torch.zeros_like(C64)
         for S in (3, 4, 5, 6):
             ms = _time(lambda: eg.einsum(0.0, "ikjl", C, 1.0, "imjn", A, "mknl", B, precision="split_bf16",
@@ -691,17 +748,19 @@ def suite_batched(eg, count=2048):
     Cs = [torch.zeros((a, b), dtype=torch.float64, device="cuda") for (i, j, a, b) in shapes]
     flop = sum(2.0 * i * j * a * b for (i, j, a, b) in shapes)
     res = {"config": f"{count} uneven contractions ab <- ija * ijb", "gflop": flop / 1e9}
-    sample = list(range(0, count, max(1, count // 16)))
+    As_np = [x.cpu().numpy() for x in As]
+    Bs_np = [x.cpu().numpy() for x in Bs]
+    refs = []
+    for k in range(count):
+        ref = np.zeros(Cs[k].shape)
+        oracle.einsum("ab", ref, 0.0, 1.0, "ija", As_np[k], "ijb", Bs_np[k])
+        refs.append(ref)
     for prec in ("fp64", "split_bf16"):
         t0 = time.perf_counter()
         plan = eg.GroupedPlan(0.0, "ab", Cs, 1.0, "ija", As, "ijb", Bs, precision=prec)
         t_plan = time.perf_counter() - t0
         ms_graph = _time(plan.execute, reps=5, warm=2)
-        errs = []
-        for k in sample:
-            ref = np.zeros(Cs[k].shape)
-            oracle.einsum("ab", ref, 0.0, 1.0, "ija", As[k].cpu().numpy(), "ijb", Bs[k].cpu().numpy())
-            errs.append(oracle.rel_fro(Cs[k].cpu().numpy(), ref))
+        errs = [oracle.rel_fro(c.cpu().numpy(), ref) for c, ref in zip(Cs, refs)]
         plan.close()
 
         def per_item():
@@ -710,7 +769,8 @@ def suite_batched(eg, count=2048):
         ms_loop = _time(per_item, reps=1, warm=1)
         res[prec] = {"grouped_graph_ms": ms_graph, "grouped_tflops": flop / ms_graph / 1e9,
                      "plan_build_s": t_plan, "one_launch_per_contraction_ms": ms_loop,
-                     "speedup_vs_per_item": ms_loop / ms_graph, "max_error_vs_oracle_sample": max(errs)}
+                     "speedup_vs_per_item": ms_loop / ms_graph, "items_checked_vs_oracle": len(errs),
+                     "max_error_vs_oracle": max(errs)}
     return res
 
 
@@ -761,7 +821,46 @@ def suite_autograd(eg, o=24, v=96):
             an = float(grad[idx])
             worst = max(worst, abs(fd - an) / max(abs(an), 1e-3 * gmax))
     res["fd_worst_relative_error"] = worst
+    res["fd_entries"] = {"t": 64, "g": 64, "h": h}
+    # the reference CPU einsum of the forward and the two adjoint patterns
+    # (every index of these patterns is in C or in both operands, so the C++
+    # generic loop and the Python plan semantics agree)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    t_np, g_np, R_np = tt.cpu().numpy(), gg.cpu().numpy(), R.cpu().numpy()
+    Cn = np.zeros((o, v, v, o))
+    oracle.einsum("mbej", Cn, 0.0, 1.0, "jnfb", t_np, "mnef", g_np)
+    dC = 2.0 * (Cn - R_np)
+    dt_ref = np.zeros_like(t_np)
+    oracle.einsum("jnfb", dt_ref, 0.0, 1.0, "mbej", dC, "mnef", g_np)
+    dg_ref = np.zeros_like(g_np)
+    oracle.einsum("mnef", dg_ref, 0.0, 1.0, "mbej", dC, "jnfb", t_np)
+    res["fp64_vs_oracle"] = {"dt": oracle.rel_fro(grads["fp64"][0].cpu().numpy(), dt_ref),
+                             "dg": oracle.rel_fro(grads["fp64"][1].cpu().numpy(), dg_ref)}
+    res["split_vs_oracle"] = {"dt": oracle.rel_fro(grads["split_bf16"][0].cpu().numpy(), dt_ref),
+                              "dg": oracle.rel_fro(grads["split_bf16"][1].cpu().numpy(), dg_ref)}
     return res
+
+
+SUITES = ("fock", "permute", "contraction", "batched", "autograd")
+
+
+def run_suites_inline(eg):
+    """Every other configuration at its full size; a failing suite records its
+    error instead of losing the headline line."""
+    import torch
+    out = {}
+    for name in SUITES:
+        t0 = time.perf_counter()
+        try:
+            r = SUITE_FNS[name](eg)
+        except Exception as exc:  # noqa: BLE001 -- reported in the line
+            r = {"error": f"{type(exc).__name__}: {exc}"}
+        r["wall_s"] = time.perf_counter() - t0
+        out[name] = r
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_suite(args):
@@ -769,9 +868,8 @@ def run_suite(args):
 
     import einsums_gb300 as eg
     torch.cuda.set_device(0)
-    which = args.suite.split(",") if args.suite != "all" else ["fock", "permute", "contraction", "batched", "autograd"]
-    fns = {"fock": suite_fock, "permute": suite_permute, "contraction": suite_contraction, "batched": suite_batched,
-           "autograd": suite_autograd}
+    which = args.suite.split(",") if args.suite != "all" else list(SUITES)
+    fns = SUITE_FNS
     sizes = tuple(int(x) for x in args.sizes.split(",")) if args.sizes else None
     for name in which:
         t0 = time.perf_counter()
@@ -786,6 +884,10 @@ def run_suite(args):
         print(json.dumps(r), flush=True)
 
 
+SUITE_FNS = {"fock": suite_fock, "permute": suite_permute, "contraction": suite_contraction, "batched": suite_batched,
+             "autograd": suite_autograd}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -797,6 +899,8 @@ def main():
     ap.add_argument("--slices", type=int, default=0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-suites", action="store_true",
+                    help="skip the other configurations that follow the headline in the same line")
     ap.add_argument("--suite", default=None,
                     help="measure the other configurations instead (all, or a comma list of "
                          "fock,permute,contraction,batched,autograd); one JSON line each")
