@@ -4,7 +4,8 @@
 ``libs/EinsumsPy/TensorAlgebra/src/Export.cpp:12-140`` and
 ``plan.execute(C_prefactor, C, AB_prefactor, A, B)`` runs it, either on
 single tensors or on equal-length lists of tensors (the list overload).
-Operands are CUDA float64 ``torch.Tensor`` objects (any strides); all work
+Operands are CUDA float64 ``torch.Tensor`` objects (any strides), or, for plans,
+host NumPy buffers that are copied in and the result copied back; all work
 goes through the C ABI of libeinsums_gb300.so on the current CUDA stream.
 
 ``einsum`` / ``permute`` mirror the C++ ``einsum(C_prefactor, Indices{...},
@@ -16,6 +17,7 @@ from __future__ import annotations
 import ctypes
 from typing import Sequence
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -172,7 +174,12 @@ class EinsumGenericPlan:
     def execute(self, C_prefactor, C, AB_prefactor, A, B, *, precision: str = "fp64", slices: int = 0,
                 tolerance: float = 1e-10, stream=None):
         """C = C_prefactor*C + AB_prefactor * A*B contracted over the plan's pattern.
-        ``C``, ``A``, ``B`` are tensors or equal-length lists of tensors."""
+        ``C``, ``A``, ``B`` are CUDA tensors or equal-length lists of them, or host buffers
+        (NumPy arrays; C writable), which are copied to the device, contracted there and
+        copied back into C -- the reference's execute also takes buffers (Export.cpp:17-32)."""
+        if _is_host(C) or _is_host(A) or _is_host(B):
+            return _execute_host(self, C_prefactor, C, AB_prefactor, A, B, precision=precision, slices=slices,
+                                 tolerance=tolerance, stream=stream)
         if isinstance(C, (list, tuple)):
             _run_batched(C_prefactor, self.C_indices, list(C), AB_prefactor, self.A_indices, list(A),
                          self.B_indices, list(B), semantics=SEMANTICS_PYTHON, precision=precision, slices=slices,
@@ -184,6 +191,70 @@ class EinsumGenericPlan:
 
     def __repr__(self):
         return f"{type(self).__name__}({self.C_indices!r} <- {self.A_indices!r} * {self.B_indices!r})"
+
+
+def _is_host(x) -> bool:
+    if isinstance(x, (list, tuple)):
+        return any(_is_host(y) for y in x)
+    return not isinstance(x, torch.Tensor)
+
+
+def _to_device(x, s):
+    """A float64 CUDA copy of a host buffer (or the tensor itself when already on the GPU),
+    copied on stream ``s`` through the library's copy entry point."""
+    if isinstance(x, torch.Tensor):
+        return x
+    arr = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    dev = torch.empty(arr.shape, dtype=torch.float64, device="cuda")
+    if arr.size:
+        _lib.check(_lib.load().eg_copy_to_device(ctypes.c_void_p(dev.data_ptr()), ctypes.c_void_p(arr.ctypes.data),
+                                                 arr.nbytes, ctypes.c_void_p(s)))
+    return dev, arr
+
+
+def _execute_host(plan, C_prefactor, C, AB_prefactor, A, B, **kw):
+    lib = _lib.load()
+    stream = kw.pop("stream", None)
+    s = _stream(stream)
+    lists = isinstance(C, (list, tuple))
+    Cs, As, Bs = (list(C), list(A), list(B)) if lists else ([C], [A], [B])
+    keep = []  # host arrays that must outlive the asynchronous copies
+    dC, dA, dB = [], [], []
+    for dst, src in ((dA, As), (dB, Bs)):
+        for x in src:
+            r = _to_device(x, s)
+            if isinstance(r, tuple):
+                keep.append(r[1])
+                r = r[0]
+            dst.append(r)
+    hosts = []
+    for x in Cs:
+        if isinstance(x, torch.Tensor):
+            dC.append(x)
+            hosts.append(None)
+            continue
+        if not isinstance(x, np.ndarray) or x.dtype != np.float64 or not x.flags.writeable:
+            raise TypeError("a host C must be a writable float64 NumPy array")
+        r = _to_device(x, s)
+        keep.append(r[1])
+        dC.append(r[0])
+        hosts.append(x)
+    if lists:
+        plan.execute(C_prefactor, dC, AB_prefactor, dA, dB, stream=stream, **kw)
+    else:
+        plan.execute(C_prefactor, dC[0], AB_prefactor, dA[0], dB[0], stream=stream, **kw)
+    outs = []
+    for d, h in zip(dC, hosts):
+        if h is None:
+            continue
+        out = np.empty(h.shape, dtype=np.float64)
+        if out.size:
+            _lib.check(lib.eg_copy_to_host(ctypes.c_void_p(out.ctypes.data), ctypes.c_void_p(d.data_ptr()),
+                                           out.nbytes, ctypes.c_void_p(s)))
+        outs.append((h, out))
+    _lib.check(lib.eg_stream_synchronize(ctypes.c_void_p(s)))
+    for h, out in outs:
+        h[...] = out
 
 
 class EinsumDotPlan(EinsumGenericPlan):
@@ -222,7 +293,12 @@ def einsum(C_prefactor, C_indices: Sequence, C, AB_prefactor, A_indices: Sequenc
            precision: str = "fp64", slices: int = 0, tolerance: float = 1e-10, only_generic: bool = False,
            stream=None) -> str:
     """C++-semantics einsum; returns the reference's AlgorithmChoice name.  C, A, B may also
-    be equal-length lists (the batched overload)."""
+    be equal-length lists (the batched overload), or BlockTensor / TiledTensor operands
+    (blocks.py: every tile combination through one block-sparse call)."""
+    from . import blocks
+    if any(blocks.is_blocked(x) for x in (C, A, B)):
+        return blocks.einsum_blocked(C_prefactor, C_indices, C, AB_prefactor, A_indices, A, B_indices, B,
+                                     precision=precision, slices=slices, tolerance=tolerance, stream=stream)
     if isinstance(C, (list, tuple)):
         alg = _run_batched(C_prefactor, list(C_indices), list(C), AB_prefactor, list(A_indices), list(A),
                            list(B_indices), list(B), semantics=SEMANTICS_CPP, precision=precision, slices=slices,
@@ -244,6 +320,27 @@ def permute(C_prefactor, C_indices: Sequence, C, A_prefactor, A_indices: Sequenc
     ec, ea = _tensor(C, "C"), _tensor(A, "A")
     _lib.check(lib.eg_permute(float(C_prefactor), _lib.labels(C_indices), ctypes.byref(ec), float(A_prefactor),
                               _lib.labels(A_indices), ctypes.byref(ea), ctypes.c_void_p(_stream(stream))))
+
+
+def fock_jk_symmetric(F, g, D, *, F_prefactor=1.0, J_prefactor=2.0, K_prefactor=-1.0, stream=None) -> None:
+    """F = F_prefactor*F + J_prefactor*J + K_prefactor*K with J = einsum(pq <- pqrs, rs) and
+    K = einsum(pq <- prqs, rs), for g with 8-fold permutational symmetry and symmetric D
+    (not checked); reads only the canonical eighth of g.  The defaults give the reference's
+    RHF update F += 2 J - K (QChemTests.cpp:300-303).  F, g, D: contiguous CUDA float64."""
+    lib = _lib.load()
+    if g.dim() != 4 or len(set(g.shape)) != 1:
+        raise _lib.DimensionError(3, "g must be n x n x n x n")
+    n = g.shape[0]
+    if tuple(D.shape) != (n, n) or tuple(F.shape) != (n, n):
+        raise _lib.DimensionError(3, "D and F must be n x n")
+    for t, name in ((F, "F"), (g, "g"), (D, "D")):
+        _tensor(t, name)
+        if not t.is_contiguous():
+            raise ValueError(f"{name} must be contiguous")
+    _check_device(F, g, D)
+    _lib.check(lib.eg_fock_jk_symmetric(float(F_prefactor), ctypes.c_void_p(F.data_ptr()), float(J_prefactor),
+                                        float(K_prefactor), ctypes.c_void_p(g.data_ptr()),
+                                        ctypes.c_void_p(D.data_ptr()), n, ctypes.c_void_p(_stream(stream))))
 
 
 def last_split_report() -> dict:

@@ -135,6 +135,22 @@ eg_status eg_einsum_batched(double C_prefactor, const int32_t *C_labels, const e
                             int32_t *algorithm_choice);
 
 /*
+ * Block-sparse einsum: item i adds AB_prefactor * A[i]*B[i] into the block C[i], one shared
+ * index pattern.  Items may name the same C block (the same view: pointer, extents and
+ * strides); its contributions add in item order.  Every distinct C block is first scaled by
+ * C_prefactor (zeroed when it is 0).  Items run in waves -- the w-th item of every C block --
+ * each wave one grouped launch as in eg_einsum_batched.  Distinct C blocks must not overlap.
+ * Replaces the block and tile loops of the reference's einsum on BlockTensor / TiledTensor
+ * operands (libs/Einsums/TensorAlgebra/include/Einsums/TensorAlgebra/Backends/BlockAlgebra.hpp:21-50,
+ * Backends/TileAlgebra.hpp:21-97), where each combination is one einsum call under a lock on
+ * its output tile.
+ */
+eg_status eg_einsum_blocks(double C_prefactor, const int32_t *C_labels, const eg_tensor *C_list, double AB_prefactor,
+                           const int32_t *A_labels, const eg_tensor *A_list, const int32_t *B_labels,
+                           const eg_tensor *B_list, int64_t count, const eg_options *opt, void *stream,
+                           int32_t *algorithm_choice);
+
+/*
  * C = C_prefactor * C + AB_prefactor * sum_i A[i] * B[i] over n contiguous doubles, without
  * allocating any device memory.  No counterpart in the reference: it is for callers that
  * cannot let a library call cudaMalloc -- applications whose device memory is owned by
@@ -149,6 +165,24 @@ eg_status eg_einsum_batched(double C_prefactor, const int32_t *C_labels, const e
  */
 eg_status eg_dot_noalloc(double C_prefactor, double *C, double AB_prefactor, const double *A, const double *B,
                          int64_t n, void *stream);
+
+/*
+ * Fock two-electron build for integrals with 8-fold permutational symmetry:
+ *   F = F_prefactor * F + J_prefactor * J + K_prefactor * K   (F not read when F_prefactor == 0)
+ *   J[p,q] = sum_rs g[p,q,r,s] D[r,s],   K[p,q] = sum_rs g[p,r,q,s] D[r,s]
+ * g: n^4 contiguous row-major doubles with g[p,q,r,s] = g[q,p,r,s] = g[p,q,s,r] = g[r,s,p,q];
+ * D and F: n x n contiguous row-major, D symmetric.  These symmetries are the caller's
+ * contract and are not checked: only the canonical eighth of g (p >= q, r >= s,
+ * pair(p,q) >= pair(r,s)) is read, and D[r,s] stands for D[s,r].  FP64 throughout, with a
+ * deterministic summation order.  Replaces the pair of einsum calls of the reference's RHF
+ * Fock build, F += 2 einsum(pq <- pqrs, rs) and F -= einsum(pq <- prqs, rs)
+ * (libs/Einsums/TensorAlgebra/tests/unit/QChemTests.cpp:300-303; dispatch
+ * Backends/Dispatch.hpp:444-560 and Backends/BaseAlgebra.hpp:85-139): J_prefactor = 2,
+ * K_prefactor = -1, F_prefactor = 1.  EG_ERROR_NOT_SUPPORTED when n is too large for the
+ * staged blocks (n above about 400).
+ */
+eg_status eg_fock_jk_symmetric(double F_prefactor, double *F, double J_prefactor, double K_prefactor, const double *g,
+                               const double *D, int64_t n, void *stream);
 
 /*
  * Grouped plan: lowers every item of a list einsum once, builds a device-side work list of

@@ -15,6 +15,7 @@ run in numpy.
     ops.zeros(shape) -> backend array
     ops.scalar(backend rank-0 array) -> float
     ops.copy_into(dst, src) (dst[...] = src)
+    ops.fock(F, TEI, D) (optional: F += 2 J - K in one call)
 """
 from __future__ import annotations
 
@@ -69,8 +70,11 @@ def rhf_mp2(ops, enuc: float, max_cycles: int = 50):
         e1 = e0
         D_prev = ops.numpy(D).copy()
         ops.copy_into(F, H_np)
-        ops.einsum("ij", F, 1.0, 2.0, "kl", D, "ijkl", TEI)
-        ops.einsum("ij", F, 1.0, -1.0, "kl", D, "ikjl", TEI)
+        if hasattr(ops, "fock"):
+            ops.fock(F, TEI, D)  # F += 2 J - K through a symmetric-integral entry point
+        else:
+            ops.einsum("ij", F, 1.0, 2.0, "kl", D, "ijkl", TEI)
+            ops.einsum("ij", F, 1.0, -1.0, "kl", D, "ikjl", TEI)
         evals = transform_and_diag()
         e0 = energy()
         diff = ops.array(ops.numpy(D) - D_prev)
