@@ -24,6 +24,8 @@ golden.json
       (``tests/test_*.py``).
     * ``known_answers``: the exact integer results asserted in
       ``Einsum1.cpp:17-88`` (and repeated over 10 tensors in ``Batched.cpp``).
+    * ``qchem_symmetry``: the symmetrizer matrix, orbitals per irrep and TEI
+      tile list of ``TEST_CASE("RHF symmetry")`` (QChemTests.cpp:417).
 """
 from __future__ import annotations
 
@@ -145,6 +147,28 @@ def qchem(unit_dir: str):
             "where": "libs/Einsums/TensorAlgebra/tests/unit/QChemTests.cpp:185-415"}
 
 
+def qchem_symmetry(unit_dir: str):
+    """The symmetry-adapted inputs of TEST_CASE("RHF symmetry") (QChemTests.cpp:417-...): the
+    7x7 matrix that forms the C2v symmetry-adapted combinations (``symm_values``), the orbitals
+    per irrep (``irrep_sizes``) and the TEI tiles the test fills (``TEI_sym.tile(...) = ...``)."""
+    text = open(os.path.join(unit_dir, "QChemTests.cpp")).read()
+    start = text.index('TEST_CASE("RHF symmetry")')
+    body = text[start:]
+    vals = re.search(r"std::vector<double>\s+symm_values\{([^}]*)\}", body).group(1)
+    symm = []
+    for tok in vals.replace("\n", " ").split(","):
+        tok = tok.strip()
+        neg = tok.startswith("-")
+        tok = tok.lstrip("-")
+        v = 1.0 / np.sqrt(2.0) if tok == "M_SQRT1_2" else float(tok)
+        symm.append(-v if neg else v)
+    sizes = [int(x) for x in re.search(r"irrep_sizes\{([^}]*)\}", body).group(1).split(",")]
+    tiles = [[int(x) for x in m.group(1).split(",")] for m in re.finditer(r"TEI_sym\.tile\(([0-9, ]+)\)\s*=", body)]
+    line = text.count("\n", 0, start) + 1
+    return {"symm": symm, "irrep_sizes": sizes, "tei_tiles": tiles,
+            "where": f"libs/Einsums/TensorAlgebra/tests/unit/QChemTests.cpp:{line}"}
+
+
 def main(ref_root: str):
     unit = os.path.join(ref_root, "libs/Einsums/TensorAlgebra/tests/unit")
     data = os.path.join(unit, "data/water_sto3g")
@@ -155,7 +179,7 @@ def main(ref_root: str):
                         TEI=read_tensor(os.path.join(data, "TEI.dat"), 4))
     golden = {"qchem": qchem(unit), "cpp_choices": cpp_choices(unit),
               "py_plans": py_plans(os.path.join(ref_root, "tests")),
-              "known_answers": known_answers(unit)}
+              "known_answers": known_answers(unit), "qchem_symmetry": qchem_symmetry(unit)}
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(golden, f, indent=1)
     print(f"cpp_choices={len(golden['cpp_choices'])} py_plans={len(golden['py_plans'])} "
