@@ -204,7 +204,7 @@ def _to_device(x, s):
     copied on stream ``s`` through the library's copy entry point."""
     if isinstance(x, torch.Tensor):
         return x
-    arr = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+    arr = np.array(x, dtype=np.float64, order="C", copy=True)  # keeps a 0-d buffer 0-d
     dev = torch.empty(arr.shape, dtype=torch.float64, device="cuda")
     if arr.size:
         _lib.check(_lib.load().eg_copy_to_device(ctypes.c_void_p(dev.data_ptr()), ctypes.c_void_p(arr.ctypes.data),
