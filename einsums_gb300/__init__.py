@@ -8,8 +8,9 @@ from . import _lib
 from .autograd import Einsum, einsum_ag
 from .blocks import BlockTensor, TiledTensor
 from .core import (ALGORITHMS, EinsumDirectProductPlan, EinsumDotPlan, EinsumGemmPlan, EinsumGemvPlan,
-                   EinsumGenericPlan, EinsumGerPlan, GroupedPlan, compile_plan, einsum, fock_jk_symmetric, last_split_report,
+                   EinsumGenericPlan, EinsumGerPlan, GroupedPlan, PermutePlan, compile_permute, compile_plan, einsum,
+                   fock_jk_symmetric, last_split_report,
                    permute)
 
-__all__ = ["compile_plan", "einsum", "permute", "fock_jk_symmetric", "BlockTensor", "TiledTensor", "GroupedPlan", "Einsum", "einsum_ag", "last_split_report", "ALGORITHMS", "EinsumGenericPlan",
+__all__ = ["compile_plan", "einsum", "permute", "compile_permute", "PermutePlan", "fock_jk_symmetric", "BlockTensor", "TiledTensor", "GroupedPlan", "Einsum", "einsum_ag", "last_split_report", "ALGORITHMS", "EinsumGenericPlan",
            "EinsumDotPlan", "EinsumDirectProductPlan", "EinsumGerPlan", "EinsumGemvPlan", "EinsumGemmPlan"]

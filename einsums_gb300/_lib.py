@@ -77,6 +77,10 @@ PROTOTYPES = {
     "eg_classify": (ctypes.c_int, [ctypes.c_int32, _i32p, ctypes.c_int32, _i32p, ctypes.c_int32, _i32p,
                                    ctypes.c_int32, _i32p]),
     "eg_permute": (ctypes.c_int, [ctypes.c_double, _i32p, _T, ctypes.c_double, _i32p, _T, ctypes.c_void_p]),
+    "eg_permute_plan_create": (ctypes.c_int, [ctypes.c_double, _i32p, _T, ctypes.c_double, _i32p, _T,
+                                              _P(ctypes.c_void_p)]),
+    "eg_permute_plan_execute": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "eg_permute_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "eg_einsum_batched": (ctypes.c_int, [ctypes.c_double, _i32p, _T, ctypes.c_double, _i32p, _T, _i32p, _T,
                                          ctypes.c_int64, _P(EgOptions), ctypes.c_void_p, _i32p]),
     "eg_einsum_blocks": (ctypes.c_int, [ctypes.c_double, _i32p, _T, ctypes.c_double, _i32p, _T, _i32p, _T,
@@ -84,7 +88,8 @@ PROTOTYPES = {
     "eg_dot_noalloc": (ctypes.c_int, [ctypes.c_double, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
     "eg_fock_jk_symmetric": (ctypes.c_int, [ctypes.c_double, ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
-                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]),
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, _P(EgOptions),
+                                            ctypes.c_void_p]),
     "eg_grouped_plan_create": (ctypes.c_int, [ctypes.c_double, _i32p, _T, ctypes.c_double, _i32p, _T, _i32p, _T,
                                               ctypes.c_int64, _P(EgOptions), ctypes.c_void_p,
                                               _P(ctypes.c_void_p), _i32p]),

@@ -322,11 +322,14 @@ def permute(C_prefactor, C_indices: Sequence, C, A_prefactor, A_indices: Sequenc
                               _lib.labels(A_indices), ctypes.byref(ea), ctypes.c_void_p(_stream(stream))))
 
 
-def fock_jk_symmetric(F, g, D, *, F_prefactor=1.0, J_prefactor=2.0, K_prefactor=-1.0, stream=None) -> None:
+def fock_jk_symmetric(F, g, D, *, F_prefactor=1.0, J_prefactor=2.0, K_prefactor=-1.0, precision="fp64",
+                      slices=0, stream=None) -> None:
     """F = F_prefactor*F + J_prefactor*J + K_prefactor*K with J = einsum(pq <- pqrs, rs) and
     K = einsum(pq <- prqs, rs), for g with 8-fold permutational symmetry and symmetric D
     (not checked); reads only the canonical eighth of g.  The defaults give the reference's
-    RHF update F += 2 J - K (QChemTests.cpp:300-303).  F, g, D: contiguous CUDA float64."""
+    RHF update F += 2 J - K (QChemTests.cpp:300-303).  F, g, D: contiguous CUDA float64.
+    precision="split_bf16" sums four of the six contributions per element as exact 8-bit
+    digit products on the FP32 pipe (last_split_report() gives the bound)."""
     lib = _lib.load()
     if g.dim() != 4 or len(set(g.shape)) != 1:
         raise _lib.DimensionError(3, "g must be n x n x n x n")
@@ -338,9 +341,55 @@ def fock_jk_symmetric(F, g, D, *, F_prefactor=1.0, J_prefactor=2.0, K_prefactor=
         if not t.is_contiguous():
             raise ValueError(f"{name} must be contiguous")
     _check_device(F, g, D)
+    opt = _options(precision, slices, SEMANTICS_CPP, False, 1e-10)
     _lib.check(lib.eg_fock_jk_symmetric(float(F_prefactor), ctypes.c_void_p(F.data_ptr()), float(J_prefactor),
                                         float(K_prefactor), ctypes.c_void_p(g.data_ptr()),
-                                        ctypes.c_void_p(D.data_ptr()), n, ctypes.c_void_p(_stream(stream))))
+                                        ctypes.c_void_p(D.data_ptr()), n, ctypes.byref(opt),
+                                        ctypes.c_void_p(_stream(stream))))
+
+
+class PermutePlan:
+    """A compiled permute (compile_permute of Permute.hpp:37-171): fixed permutation, shapes,
+    strides and prefactors; ``execute(C, A)`` runs it on any tensors with those shapes and
+    strides (the reference's permute(&C, A, plan), Permute.hpp:292-297)."""
+
+    def __init__(self, C_prefactor, C_indices: Sequence, C, A_prefactor, A_indices: Sequence, A):
+        lib = _lib.load()
+        C_indices, A_indices = list(C_indices), list(A_indices)
+        if C.dim() != len(C_indices) or A.dim() != len(A_indices):
+            raise _lib.RankError(2, "tensor ranks do not match the indices")
+        self._shape = (tuple(C.shape), tuple(C.stride()), tuple(A.shape), tuple(A.stride()))
+        ec, ea = _tensor(C, "C"), _tensor(A, "A")
+        h = ctypes.c_void_p()
+        _lib.check(lib.eg_permute_plan_create(float(C_prefactor), _lib.labels(C_indices), ctypes.byref(ec),
+                                              float(A_prefactor), _lib.labels(A_indices), ctypes.byref(ea),
+                                              ctypes.byref(h)))
+        self._h = h
+
+    def execute(self, C, A, *, stream=None) -> None:
+        if (tuple(C.shape), tuple(C.stride()), tuple(A.shape), tuple(A.stride())) != self._shape:
+            raise _lib.DimensionError(3, "C and A must have the plan's shapes and strides")
+        _tensor(C, "C")
+        _tensor(A, "A")
+        _check_device(C, A)
+        _lib.check(_lib.load().eg_permute_plan_execute(self._h, ctypes.c_void_p(C.data_ptr() if C.numel() else None),
+                                                       ctypes.c_void_p(A.data_ptr() if A.numel() else None),
+                                                       ctypes.c_void_p(_stream(stream))))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.load().eg_permute_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 -- interpreter shutdown
+            pass
+
+
+def compile_permute(C_prefactor, C_indices: Sequence, C, A_prefactor, A_indices: Sequence, A) -> PermutePlan:
+    return PermutePlan(C_prefactor, C_indices, C, A_prefactor, A_indices, A)
 
 
 def last_split_report() -> dict:

@@ -385,13 +385,13 @@ eg_status lower_for_group(double cp, const int32_t *Cl, const eg_tensor *C, doub
     return EG_SUCCESS;
 }
 
-eg_status permute_impl(double cp, const int32_t *Cl, const eg_tensor *C, double ap, const int32_t *Al,
-                       const eg_tensor *A, cudaStream_t stream) {
+eg_status build_permute_desc(double cp, const int32_t *Cl, const eg_tensor *C, double ap, const int32_t *Al,
+                             const eg_tensor *A, PermuteDesc &p) {
     eg_status st;
     if ((st = check_tensor(C, Cl, "C")) != EG_SUCCESS) return st;
     if ((st = check_tensor(A, Al, "A")) != EG_SUCCESS) return st;
     if (C->rank != A->rank) return fail(EG_ERROR_RANK, "permute: C and A ranks differ");
-    PermuteDesc p;
+    p = PermuteDesc{};
     p.rank = C->rank;
     p.A = A->data;
     p.C = C->data;
@@ -417,6 +417,14 @@ eg_status permute_impl(double cp, const int32_t *Cl, const eg_tensor *C, double 
         for (int d = 0; d < C->rank; d++) count += (Cl[d] == Al[j]);
         if (count != 1) return fail(EG_ERROR_INVALID_ARGUMENT, "permute: every A index must occur exactly once in C");
     }
+    return EG_SUCCESS;
+}
+
+eg_status permute_impl(double cp, const int32_t *Cl, const eg_tensor *C, double ap, const int32_t *Al,
+                       const eg_tensor *A, cudaStream_t stream) {
+    PermuteDesc p;
+    const eg_status st = build_permute_desc(cp, Cl, C, ap, Al, A, p);
+    if (st != EG_SUCCESS) return st;
     return launch_permute(p, stream);
 }
 

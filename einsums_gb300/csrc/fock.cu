@@ -18,36 +18,51 @@
 //   T1 YJ[p,q] += f g D[r,s]   T2 YJ[r,s] += f g D[p,q]   T3 XK[p,r] += f g D[q,s]
 //   T4 XK[q,r] += f g D[p,s]   T5 XK[p,s] += f g D[q,r]   T6 XK[q,s] += f g D[p,r]
 //
-// Six FP64 multiply-adds per canonical element, 0.75 n^4 in all, against
-// 2 n^4 for the two general contractions.  On this GPU those multiply-adds,
-// not HBM, bound the build: the FP64 pipe retires about one warp-wide FMA
-// per 64 cycles per SM sub-partition, so every kernel here keeps the FP64
-// instructions to the multiply-adds themselves and does its index arithmetic,
-// degeneracy scaling (exponent decrements) and loads on the other pipes.
+// Six multiply-adds per canonical element, 0.75 n^4 in all, against 2 n^4 for
+// the two general contractions.  On this GPU the FP64 pipe retires about one
+// warp-wide FMA per 64 cycles per SM sub-partition, a sixty-fourth of the FP32
+// rate, so those multiply-adds bound the FP64 form.  The split form moves four
+// of the six terms (T1, T2, T4, T5) to the FP32 pipe: g and D are cut into S
+// balanced 8-bit digits at a power-of-two scale per summed line -- the digits
+// of the split-BF16 contraction (split.cuh) -- whose products, integers below
+// 2^14, add up exactly in FP32 over at most 64 elements and then exactly in
+// integers (Horner over the digit groups d = s + t < S), converted to FP64
+// once per line.  T3 and T6 stay FP64 and run on the FP64 pipe beside them.
 //
-// Kernels (no atomics: every partial has one home and the last pass sums
-// them in a fixed order, so the result is deterministic):
-//   k_fock_pair_blocks      one CTA per (p, r, chunk of 64 q): the block
-//                           B[q,s] = g[p,q,r,s] is staged in shared memory;
-//                           row sums give T1 and T4, column sums T2, T5 and
-//                           the block total T3.
-//   k_fock_exchange_blocks  one CTA per (q, s): the weighted total T6 of the
-//                           block g[q,p,s,r] (= g[p,q,r,s]) over (p, r).
-//   k_fock_reduce           one CTA per output row: sums the partials of
-//                           YJ and XK.
-//   k_fock_combine          applies J = 2 (YJ + YJ^T), K = XK + XK^T and the
-//                           prefactors.
+// Every pass is a set of sums along lines of g read by 32 lanes at 32
+// consecutive addresses: the symmetries of g give each sum a layout whose
+// fastest index is the lanes' own.  Each lane keeps its sums in registers; no
+// shared-memory tiles, no atomics.  Every partial has one home and the last
+// passes add them in a fixed order, so the result is deterministic.
+//   k_fock_digits_d   (split form) the digits of every row of D.
+//   k_fock_rows<S>    warp (p, r, 32 q): T1 and T4, sums over s of
+//                     g[r,s,p,q] (= g[p,q,r,s]), lanes along q.
+//   k_fock_cols<S>    warp (p, r, 32 s): T2, T5 and T3, sums over q of
+//                     g[p,q,r,s], lanes along s.
+//   k_fock_exchange   CTA (q, 32 s, quarter of p): T6, sums over (p, r) of
+//                     g[q,p,r,s] (= g[p,q,r,s]) D[p,r], lanes along s.
+//   k_fock_reduce     one CTA per output row: YJ and XK from the partials.
+//   k_fock_combine    J = 2 (YJ + YJ^T), K = XK + XK^T and the prefactors.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 
-#include "common.cuh"
+#include "split.cuh"
 
 namespace eg {
+void set_split_report(const eg_split_report &r);
 
 namespace {
 
-constexpr int kFockThreads = 128;
-constexpr int kFockChunk = 64; // rows q of a pair block staged per CTA
+using split::int_times_pow2_rn;
+using split::scaled_round;
+
+constexpr int kWarps = 4;      // warps per CTA of the line passes (consecutive r)
+constexpr int kExPSplit = 4;   // exchange CTAs over the p range of one (q, 32 s)
+constexpr int kRedWarps = 8;   // warps of a reduction CTA
+constexpr int kFockMaxN = 384; // g is 174 GB at n = 384
+constexpr int kFlush = 64;     // elements per exact FP32 digit-group sum (a multiple of kBatch)
+constexpr int kBatch = 8;      // independent loads in flight per lane in the line passes
 
 // x / 2, exactly: an exponent decrement for normal numbers, else a multiply.
 __device__ __forceinline__ double half_exact(double x) {
@@ -56,182 +71,408 @@ __device__ __forceinline__ double half_exact(double x) {
     return x * 0.5;
 }
 
+// Scale exponent of a set whose largest |x| has IEEE bits mx: |x| < 2^e
+// (0 for an all-zero set, INT_MIN when it holds an Inf or NaN).
+__device__ __forceinline__ int set_exponent(unsigned long long mx) {
+    const int ex = (int)(mx >> 52);
+    if (ex == 0x7ff) return INT_MIN;
+    if (mx == 0) return 0;
+    if (ex != 0) return ex - 1022;
+    int e = 0;
+    frexp(__longlong_as_double((long long)mx), &e); // subnormal maximum
+    return e;
+}
+
+// The S balanced digits of round(x 2^sh) as floats, most significant first:
+// with the bias B = 127 (256^(S-2) + ... + 1) the lower digits are plain bytes
+// of F + B, each made a float exactly as (2^23 + u) - (2^23 + 127), and the top
+// digit is (F + B) >> 8 (S - 1) -- the digits of split.cuh's digits_bf16x2.
+template <int S>
+__device__ __forceinline__ void digits_f32(double x, int sh, float (&f)[S]) {
+    constexpr long long bias = [] {
+        long long b = 0;
+        for (int s = 1; s < S; s++) b = b * 256 + 127;
+        return b;
+    }();
+    const long long G = scaled_round(x, sh) + bias;
+    const uint32_t w[2] = {(uint32_t)G, (uint32_t)((unsigned long long)G >> 32)};
+#pragma unroll
+    for (int s = 1; s < S; s++) {
+        const int byte = S - 1 - s;
+        const uint32_t u = (w[byte >> 2] >> (8 * (byte & 3))) & 255u;
+        f[s] = __uint_as_float(0x4B000000u | u) - 8388735.0f;
+    }
+    const int t0 = (int)(G >> (8 * (S - 1)));
+    f[0] = __int_as_float(0x4B400000 + t0) - 12582912.0f;
+}
+
+// acc[d] += sum_{s + t = d} a[s] b[t] for d < S: the triangular digit product.
+template <int S>
+__device__ __forceinline__ void digit_fma(const float (&a)[S], const float (&b)[S], float (&acc)[S]) {
+#pragma unroll
+    for (int d = 0; d < S; d++)
+#pragma unroll
+        for (int s = 0; s <= d; s++) acc[d] = fmaf(a[s], b[d - s], acc[d]);
+}
+
+// The FP32 group sums (integers below 2^24) folded into int32 running sums.
+template <int S>
+__device__ __forceinline__ void digit_flush(float (&acc)[S], int (&run)[S]) {
+#pragma unroll
+    for (int d = 0; d < S; d++) {
+        run[d] += __float2int_rn(acc[d]);
+        acc[d] = 0.0f;
+    }
+}
+
+// The FP64 value of sum_d run[d] 256^(S-1-d) 2^e (INT_MIN: NaN).
+template <int S>
+__device__ __forceinline__ double digit_value(const int (&run)[S], int e) {
+    if (e == INT_MIN) return __longlong_as_double(0x7ff8000000000000ll);
+    long long R = 0;
+#pragma unroll
+    for (int d = 0; d < S; d++) R = R * 256 + run[d];
+    return int_times_pow2_rn(R, e);
+}
+
+template <int S>
+__device__ __forceinline__ void load_digits(const float *p, float (&b)[S]) {
+#pragma unroll
+    for (int t = 0; t < S; t++) b[t] = __ldg(p + t);
+}
+
 struct FockScratch {
-    double *S1;  // [p][r][q]      T1 row sums
-    double *S4;  // [q][p][r]      T4 row sums
-    double *S2;  // [r][p][c][s]   T2 column sums of chunk c
-    double *S5;  // [p][r][c][s]   T5 column sums of chunk c
-    double *X3;  // [p][r][c]      T3 totals of chunk c
-    double *X6;  // [q][s]         T6 totals
-    double *YJ;  // [i][j], i >= j  combined T1 + T2
-    double *XK;  // [i][j]          combined T3..T6
+    double *S1;      // [p][r][q]   T1: sum over s
+    double *S4;      // [q][p][r]   T4: sum over s
+    double *S2;      // [r][p][s]   T2: sum over q
+    double *S5;      // [p][r][s]   T5: sum over q
+    double *X3;      // [p][r][sc]  T3: per chunk of 32 s
+    double *X6;      // [q][ps][s]  T6: per quarter of p
+    double *YJ;      // [i][j], i >= j
+    double *XK;      // [i][j]
+    const float *Dd; // split form: [row][k][S] digits of D
+    const int *De;   //             [row] scale exponents of D's rows
+    int nsc;         // chunks of 32 s
 };
 
-// Pair block (p, r), p >= r, rows q in chunk c.  Unit index x runs the pairs
-// from the largest p down so that the big blocks start first.
-__global__ void __launch_bounds__(kFockThreads) k_fock_pair_blocks(const double *__restrict__ g,
-                                                                   const double *__restrict__ D, int n, int nc,
-                                                                   FockScratch sc) {
-    extern __shared__ double sm[];
-    const int npairs = n * (n + 1) / 2;
-    const int x = npairs - 1 - (int)blockIdx.x;
-    int p = (int)((sqrtf(8.0f * (float)x + 1.0f) - 1.0f) * 0.5f);
-    while ((p + 1) * (p + 2) / 2 <= x) p++;
-    while (p * (p + 1) / 2 > x) p--;
-    const int r = x - p * (p + 1) / 2;
-    const int c = blockIdx.y;
-    const int q0 = c * kFockChunk;
-    if (q0 > p) return;
-    const int nq = min(kFockChunk, p + 1 - q0);
-    const int ns = r + 1;
-    const int ld = ns | 1; // odd row stride: rows of the column walk fall in different banks
-    double *T = sm;                      // [nq][ld]
-    double *Dr = T + kFockChunk * ld;    // D[r][0..n)
-    double *Dp = Dr + n;                 // D[p][0..n)
-    const int tid = threadIdx.x;
-    for (int i = tid; i < n; i += kFockThreads) {
-        Dr[i] = __ldg(D + (size_t)r * n + i);
-        Dp[i] = __ldg(D + (size_t)p * n + i);
+// Unit x of the line passes, the largest p first: (p, group of kWarps r).
+__device__ __forceinline__ void unit_pr(int x, int n, int &p, int &rg) {
+    int total = 0;
+    for (int pp = 0; pp < n; pp++) total += (pp + kWarps) / kWarps;
+    x = total - 1 - x;
+    int cum = 0;
+    for (p = 0; p < n; p++) {
+        const int c = (p + kWarps) / kWarps;
+        if (x < cum + c) break;
+        cum += c;
     }
-    // Stage the block with its degeneracy factors.  Row q, columns s <= r (s <= q
-    // when p == r, the rest of the row zero).
-    const bool diag = p == r;
-    for (int e = tid; e < nq * ns; e += kFockThreads) {
-        const int ql = e / ns, s = e - ql * ns;
-        const int q = q0 + ql;
-        double v = 0.0;
-        if (!diag || s <= q) {
-            v = __ldcs(g + (((size_t)p * n + q) * n + r) * n + s);
-            if (q == p) v = half_exact(v);
-            if (s == r) v = half_exact(v);
-            if (diag && s == q) v = half_exact(v);
-        }
-        T[ql * ld + s] = v;
-    }
+    rg = x - cum;
+}
+
+// Digits of every row of D at the row's own scale: De[row] with |D[row][k]| < 2^e.
+template <int S>
+__global__ void __launch_bounds__(128) k_fock_digits_d(const double *__restrict__ D, int n, float *Dd, int *De) {
+    const int row = blockIdx.x;
+    __shared__ unsigned long long red[4];
+    unsigned long long mx = 0;
+    for (int k = threadIdx.x; k < n; k += 128) mx = max(mx, split::abs_bits(D[(size_t)row * n + k]));
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
     __syncthreads();
-    // Rows: two threads per row split the columns; T1 with D[r][s], T4 with D[p][s].
-    {
-        const int ql = tid >> 1, h = tid & 1;
+    mx = max(max(red[0], red[1]), max(red[2], red[3]));
+    const int e = set_exponent(mx);
+    if (threadIdx.x == 0) De[row] = e;
+    const int sh = split::kTopBits + split::kBits * (S - 1) - (e == INT_MIN ? 0 : e);
+    for (int k = threadIdx.x; k < n; k += 128) {
+        float f[S];
+        digits_f32<S>(e == INT_MIN ? 0.0 : D[(size_t)row * n + k], sh, f);
+#pragma unroll
+        for (int t = 0; t < S; t++) Dd[((size_t)row * n + k) * S + t] = f[t];
+    }
+}
+
+constexpr int kShift(int S) { return -2 * split::kTopBits - split::kBits * (S - 1); }
+
+// T1 and T4.  Warp (p, r), lane q: sums over s <= r (s <= q when p == r) of
+// f g[p,q,r,s] {D[r,s], D[p,s]}, reading g[r,s,p,q] -- lanes along q.  The
+// loop runs over the warp's common range in batches of kBatch independent
+// loads (a lane outside its own range adds nothing), so that each warp keeps
+// kBatch reads in flight instead of one.
+template <int S>
+__global__ void __launch_bounds__(kWarps * 32) k_fock_rows(const double *__restrict__ g,
+                                                           const double *__restrict__ D, int n, FockScratch sc) {
+    int p, rg;
+    unit_pr(blockIdx.x, n, p, rg);
+    const int r = rg * kWarps + (threadIdx.x >> 5);
+    const int q = blockIdx.y * 32 + (threadIdx.x & 31);
+    if (r > p || (int)blockIdx.y * 32 > p) return; // whole warps leave together
+    const bool on = q <= p;
+    const bool diag = p == r;
+    const int smax = diag ? q : r; // this lane's last s
+    const size_t step = (size_t)n * n; // s -> s + 1 in g[r][s][p][q]
+    const double *gl = g + (((size_t)r * n) * n + p) * n + (on ? q : p);
+    const double *Dr = D + (size_t)r * n, *Dp = D + (size_t)p * n;
+    auto scale = [&](double v, int s) {
+        if (q == p) v = half_exact(v);
+        if (s == r) v = half_exact(v);
+        if (diag && s == q) v = half_exact(v);
+        return v;
+    };
+    double v1 = 0.0, v4 = 0.0;
+    if constexpr (S == 0) {
         double a1 = 0.0, a4 = 0.0;
-        if (ql < nq) {
-            const double *row = T + ql * ld;
-            for (int s = h; s < ns; s += 2) {
-                const double v = row[s];
-                a1 = fma(v, Dr[s], a1);
-                a4 = fma(v, Dp[s], a4);
+        for (int s0 = 0; s0 <= r; s0 += kBatch) {
+            double v[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) v[u] = s0 + u <= r ? __ldcs(gl + (s0 + u) * step) : 0.0;
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) {
+                const int s = s0 + u;
+                if (s <= smax && on) {
+                    const double w = scale(v[u], s);
+                    a1 = fma(w, __ldg(Dr + s), a1);
+                    a4 = fma(w, __ldg(Dp + s), a4);
+                }
             }
         }
-        a1 += __shfl_xor_sync(0xffffffffu, a1, 1);
-        a4 += __shfl_xor_sync(0xffffffffu, a4, 1);
-        if (ql < nq && h == 0) {
-            const int q = q0 + ql;
-            sc.S1[((size_t)p * n + r) * n + q] = a1;
-            sc.S4[((size_t)q * n + p) * n + r] = a4;
+        v1 = a1;
+        v4 = a4;
+    } else {
+        unsigned long long mx = 0;
+        for (int s0 = 0; s0 <= r; s0 += kBatch) {
+            unsigned long long b[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) b[u] = s0 + u <= r ? split::abs_bits(__ldg(gl + (s0 + u) * step)) : 0ull;
+#pragma unroll
+            for (int u = 0; u < kBatch; u++)
+                if (s0 + u <= smax) mx = max(mx, b[u]);
         }
+        const int e = set_exponent(mx);
+        const int sh = split::kTopBits + split::kBits * (S - 1) - (e == INT_MIN ? 0 : e);
+        float acc1[S] = {}, acc4[S] = {};
+        int run1[S] = {}, run4[S] = {};
+        const float *Drd = sc.Dd + (size_t)r * n * S, *Dpd = sc.Dd + (size_t)p * n * S;
+        for (int s0 = 0; s0 <= r; s0 += kBatch) {
+            double v[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) v[u] = s0 + u <= r ? __ldcs(gl + (s0 + u) * step) : 0.0;
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) {
+                const int s = s0 + u;
+                if (s <= smax && on) {
+                    float a[S], w[S];
+                    digits_f32<S>(e == INT_MIN ? 0.0 : scale(v[u], s), sh, a);
+                    load_digits<S>(Drd + s * S, w);
+                    digit_fma<S>(a, w, acc1);
+                    load_digits<S>(Dpd + s * S, w);
+                    digit_fma<S>(a, w, acc4);
+                }
+            }
+            if (((s0 + kBatch) % kFlush) == 0) { // every kFlush elements: exact FP32 group sums
+                digit_flush<S>(acc1, run1);
+                digit_flush<S>(acc4, run4);
+            }
+        }
+        digit_flush<S>(acc1, run1);
+        digit_flush<S>(acc4, run4);
+        const int eDr = __ldg(sc.De + r), eDp = __ldg(sc.De + p);
+        v1 = digit_value<S>(run1, (e == INT_MIN || eDr == INT_MIN) ? INT_MIN : e + eDr + kShift(S));
+        v4 = digit_value<S>(run4, (e == INT_MIN || eDp == INT_MIN) ? INT_MIN : e + eDp + kShift(S));
     }
-    // Columns: T2 with D[p][q], T5 with D[q][r] = D[r][q], T3 with D[q][s].
-    double a3 = 0.0;
-    for (int s = tid; s < ns; s += kFockThreads) {
+    if (on) {
+        sc.S1[((size_t)p * n + r) * n + q] = v1;
+        sc.S4[((size_t)q * n + p) * n + r] = v4;
+    }
+}
+
+// T2, T5 and T3.  Warp (p, r), lane s <= r: sums over q <= p (q >= s when p == r)
+// of f g[p,q,r,s] {D[p,q], D[r,q], D[q,s]} -- lanes along s, batches of
+// kBatch loads as in the rows pass.  T3 adds up across the warp (one total per
+// chunk of 32 s).
+template <int S>
+__global__ void __launch_bounds__(kWarps * 32) k_fock_cols(const double *__restrict__ g,
+                                                           const double *__restrict__ D, int n, FockScratch sc) {
+    int p, rg;
+    unit_pr(blockIdx.x, n, p, rg);
+    const int r = rg * kWarps + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    const int s = blockIdx.y * 32 + lane;
+    if (r > p || (int)blockIdx.y * 32 > r) return; // whole warps leave together
+    const bool on = s <= r;
+    const bool diag = p == r;
+    const int qmin = diag ? s : 0; // this lane's first q
+    const size_t step = (size_t)n * n; // q -> q + 1 in g[p][q][r][s]
+    const double *gl = g + (((size_t)p * n) * n + r) * n + (on ? s : r);
+    const double *Dp = D + (size_t)p * n, *Dr = D + (size_t)r * n;
+    auto scale = [&](double v, int q) {
+        if (q == p) v = half_exact(v);
+        if (s == r) v = half_exact(v);
+        if (diag && s == q) v = half_exact(v);
+        return v;
+    };
+    double a3 = 0.0, v2 = 0.0, v5 = 0.0;
+    if constexpr (S == 0) {
         double a2 = 0.0, a5 = 0.0;
-        for (int ql = 0; ql < nq; ql++) {
-            const double v = T[ql * ld + s];
-            const int q = q0 + ql;
-            a2 = fma(v, Dp[q], a2);
-            a5 = fma(v, Dr[q], a5);
-            a3 = fma(v, __ldg(D + (size_t)q * n + s), a3);
+        for (int q0 = 0; q0 <= p; q0 += kBatch) {
+            double v[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) v[u] = q0 + u <= p ? __ldcs(gl + (q0 + u) * step) : 0.0;
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) {
+                const int q = q0 + u;
+                if (q <= p && q >= qmin && on) {
+                    const double w = scale(v[u], q);
+                    a2 = fma(w, __ldg(Dp + q), a2);
+                    a5 = fma(w, __ldg(Dr + q), a5);
+                    a3 = fma(w, __ldg(D + (size_t)q * n + s), a3);
+                }
+            }
         }
-        sc.S2[(((size_t)r * n + p) * nc + c) * n + s] = a2;
-        sc.S5[(((size_t)p * n + r) * nc + c) * n + s] = a5;
+        v2 = a2;
+        v5 = a5;
+    } else {
+        unsigned long long mx = 0;
+        for (int q0 = 0; q0 <= p; q0 += kBatch) {
+            unsigned long long b[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) b[u] = q0 + u <= p ? split::abs_bits(__ldg(gl + (q0 + u) * step)) : 0ull;
+#pragma unroll
+            for (int u = 0; u < kBatch; u++)
+                if (q0 + u >= qmin) mx = max(mx, b[u]);
+        }
+        const int e = set_exponent(mx);
+        const int sh = split::kTopBits + split::kBits * (S - 1) - (e == INT_MIN ? 0 : e);
+        float acc2[S] = {}, acc5[S] = {};
+        int run2[S] = {}, run5[S] = {};
+        const float *Dpd = sc.Dd + (size_t)p * n * S, *Drd = sc.Dd + (size_t)r * n * S;
+        for (int q0 = 0; q0 <= p; q0 += kBatch) {
+            double v[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) v[u] = q0 + u <= p ? __ldcs(gl + (q0 + u) * step) : 0.0;
+#pragma unroll
+            for (int u = 0; u < kBatch; u++) {
+                const int q = q0 + u;
+                if (q <= p && q >= qmin && on) {
+                    const double w = scale(v[u], q);
+                    float a[S], b[S];
+                    digits_f32<S>(e == INT_MIN ? 0.0 : w, sh, a);
+                    load_digits<S>(Dpd + q * S, b);
+                    digit_fma<S>(a, b, acc2);
+                    load_digits<S>(Drd + q * S, b);
+                    digit_fma<S>(a, b, acc5);
+                    a3 = fma(w, __ldg(D + (size_t)q * n + s), a3);
+                }
+            }
+            if (((q0 + kBatch) % kFlush) == 0) {
+                digit_flush<S>(acc2, run2);
+                digit_flush<S>(acc5, run5);
+            }
+        }
+        digit_flush<S>(acc2, run2);
+        digit_flush<S>(acc5, run5);
+        const int eDp = __ldg(sc.De + p), eDr = __ldg(sc.De + r);
+        v2 = digit_value<S>(run2, (e == INT_MIN || eDp == INT_MIN) ? INT_MIN : e + eDp + kShift(S));
+        v5 = digit_value<S>(run5, (e == INT_MIN || eDr == INT_MIN) ? INT_MIN : e + eDr + kShift(S));
     }
-    __shared__ double red[kFockThreads / 32];
+    if (on) {
+        sc.S2[((size_t)r * n + p) * n + s] = v2;
+        sc.S5[((size_t)p * n + r) * n + s] = v5;
+    }
     for (int o = 16; o > 0; o >>= 1) a3 += __shfl_down_sync(0xffffffffu, a3, o);
-    if ((tid & 31) == 0) red[tid >> 5] = a3;
-    __syncthreads();
-    if (tid == 0) {
-        double t = 0.0;
-        for (int w = 0; w < kFockThreads / 32; w++) t += red[w];
-        sc.X3[((size_t)p * n + r) * nc + c] = t;
-    }
+    if (lane == 0) sc.X3[((size_t)p * n + r) * sc.nsc + blockIdx.y] = a3;
 }
 
-// Exchange block (q, s): T6 = sum over canonical (p, r) with p >= q, r >= s of
-// f g[q,p,s,r] D[p,r].  Rows p in [max(q, s), n); row p holds r in [s, p],
-// without r = p when q < s (then pair(p,q) < pair(p,s)).  The rows are walked
-// as one flattened index so that short rows leave no lanes idle.
-__global__ void __launch_bounds__(kFockThreads) k_fock_exchange_blocks(const double *__restrict__ g,
-                                                                       const double *__restrict__ D, int n,
-                                                                       double *__restrict__ X6) {
-    const int u = n * n - 1 - (int)blockIdx.x; // small (q, s) -- the big blocks -- first
-    const int q = u / n, s = u - q * n;
-    const int p0 = max(q, s);
-    const int drop = q < s ? 1 : 0;
-    const int L0 = p0 - s + 1 - drop; // length of row p0; row p0 + i has L0 + i elements
-    const int rows = n - p0;
-    const long long total = (long long)rows * L0 + (long long)rows * (rows - 1) / 2;
-    const double *gq = g + ((size_t)q * n) * n * n;
+// T6: XK[q,s] = sum over canonical (p, r) -- p >= q, s <= r <= p, without r = p
+// when q < s -- of f g[q,p,r,s] D[p,r].  CTA (q, 32 s, quarter ps of p): lane = s,
+// warps interleaved over p; the four warps' sums are added in warp order.
+__global__ void __launch_bounds__(kWarps * 32) k_fock_exchange(const double *__restrict__ g,
+                                                               const double *__restrict__ D, int n, int nsc,
+                                                               double *__restrict__ X6) {
+    const int q = blockIdx.x / nsc, s0 = (blockIdx.x - q * nsc) * 32;
+    const int ps = blockIdx.y;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int s = s0 + lane;
+    __shared__ double part[kWarps][32];
     double acc = 0.0;
-    // (i, off): row and position of flattened index k; rows are walked forward
-    // as k advances (integer work only: the FP64 pipe is kept for the sums)
-    long long k = threadIdx.x, off = k;
-    int i = 0;
-    while (i < rows && off >= L0 + i) {
-        off -= L0 + i;
-        i++;
-    }
-    for (; k < total; k += kFockThreads) {
-        const int p = p0 + i;
-        const int rr = s + (int)off;
-        double v = __ldcs(gq + ((size_t)p * n + s) * n + rr);
-        if (p == q) v = half_exact(v);
-        if (rr == s) v = half_exact(v);
-        if (p == rr && q == s) v = half_exact(v);
-        acc = fma(v, __ldg(D + (size_t)p * n + rr), acc);
-        off += kFockThreads;
-        while (i < rows && off >= L0 + i) {
-            off -= L0 + i;
-            i++;
+    {
+        // the warp walks r over [s0, p] in batches of kBatch loads; a lane adds only
+        // its canonical r in [s, rend]
+        const int sl = s < n ? s : n - 1;
+        for (int p = max(q, s0) + ps + kExPSplit * warp; p < n; p += kExPSplit * kWarps) {
+            const int rend = s >= n ? -1 : (q < s ? p - 1 : p);
+            const double *gl = g + (((size_t)q * n + p) * n) * n + sl;
+            const double *Dp = D + (size_t)p * n;
+            for (int r0 = s0; r0 <= p; r0 += kBatch) {
+                double v[kBatch];
+#pragma unroll
+                for (int u = 0; u < kBatch; u++) v[u] = r0 + u <= p ? __ldcs(gl + (size_t)(r0 + u) * n) : 0.0;
+#pragma unroll
+                for (int u = 0; u < kBatch; u++) {
+                    const int r = r0 + u;
+                    if (r >= s && r <= rend) {
+                        double w = v[u];
+                        if (p == q) w = half_exact(w);
+                        if (r == s) w = half_exact(w);
+                        if (p == r && q == s) w = half_exact(w);
+                        acc = fma(w, __ldg(Dp + r), acc);
+                    }
+                }
+            }
         }
     }
-    __shared__ double red[kFockThreads / 32];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    part[warp][lane] = acc;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < kFockThreads / 32; w++) t += red[w];
-        X6[(size_t)q * n + s] = t;
+    if (warp == 0 && s < n) {
+        double t = part[0][lane];
+        for (int w = 1; w < kWarps; w++) t += part[w][lane];
+        X6[((size_t)q * kExPSplit + ps) * n + s] = t;
     }
 }
 
-// Row i of YJ (j <= i) and XK from the partials: one thread per j, so that
-// every partial row is read contiguously; each sum runs in a fixed order.
-__global__ void __launch_bounds__(kFockThreads) k_fock_reduce(int n, int nc, FockScratch sc) {
+// Row i, columns j of one chunk of 32, of YJ (j <= i) and XK from the partials.
+// Lanes run over j (every read is contiguous); warp w takes the terms t = w,
+// w + 8, ... of each sum over p or r, and the eight warps' sums are added in
+// warp order.
+__global__ void __launch_bounds__(kRedWarps * 32) k_fock_reduce(int n, FockScratch sc) {
+    __shared__ double sr[2][kRedWarps][32];
     const int i = blockIdx.x;
-    for (int j = threadIdx.x; j < n; j += kFockThreads) {
-        // XK[i][j]: T6, then T4 over pair blocks (p, r = j) with p >= max(i, j)
-        double xa = sc.X6[(size_t)i * n + j], xb = 0.0;
-        for (int p = max(i, j); p < n; p++) xb += sc.S4[((size_t)i * n + p) * n + j];
-        if (i >= j) {
-            // T3 over the chunks of pair block (i, j); T5 over pair blocks (i, r), j <= r <= i
-            for (int c = 0; c * kFockChunk <= i; c++) xa += sc.X3[((size_t)i * n + j) * nc + c];
-            for (int r = j; r <= i; r++)
-                for (int c = 0; c * kFockChunk <= i; c++) xb += sc.S5[(((size_t)i * n + r) * nc + c) * n + j];
-            // YJ[i][j]: T1 over pair blocks (i, r), r <= i; T2 over pair blocks (p, i), p >= i
-            double ya = 0.0, yb = 0.0;
-            for (int r = 0; r <= i; r++) ya += sc.S1[((size_t)i * n + r) * n + j];
-            for (int p = i; p < n; p++)
-                for (int c = 0; c * kFockChunk <= p; c++) yb += sc.S2[(((size_t)i * n + p) * nc + c) * n + j];
-            sc.YJ[(size_t)i * n + j] = ya + yb;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j = blockIdx.y * 32 + lane;
+    if (j < n) {
+        double xk = 0.0, yj = 0.0;
+        if (warp == 0) {
+            for (int ps = 0; ps < kExPSplit; ps++) xk += sc.X6[((size_t)i * kExPSplit + ps) * n + j];
+            if (i >= j)
+                for (int c = 0; c * 32 <= j; c++) xk += sc.X3[((size_t)i * n + j) * sc.nsc + c];
         }
-        sc.XK[(size_t)i * n + j] = xa + xb;
+        for (int t = warp; t < n; t += kRedWarps) {
+            if (t >= max(i, j)) xk += sc.S4[((size_t)i * n + t) * n + j]; // T4 of (p = t, r = j), q = i
+            if (i >= j) {
+                if (t >= j && t <= i) xk += sc.S5[((size_t)i * n + t) * n + j]; // T5 of (p = i, r = t), s = j
+                if (t <= i) yj += sc.S1[((size_t)i * n + t) * n + j];           // T1 of (p = i, r = t), q = j
+                if (t >= i) yj += sc.S2[((size_t)i * n + t) * n + j];           // T2 of (p = t, r = i), s = j
+            }
+        }
+        sr[0][warp][lane] = xk;
+        sr[1][warp][lane] = yj;
+    }
+    __syncthreads();
+    if (warp == 0 && j < n) {
+        double xk = 0.0, yj = 0.0;
+        for (int w = 0; w < kRedWarps; w++) {
+            xk += sr[0][w][lane];
+            yj += sr[1][w][lane];
+        }
+        sc.XK[(size_t)i * n + j] = xk;
+        if (i >= j) sc.YJ[(size_t)i * n + j] = yj;
     }
 }
 
 // F = fp F + jp J + kp K with J = 2 (YJ + YJ^T) and K = XK + XK^T.
-__global__ void __launch_bounds__(kFockThreads) k_fock_combine(double *F, int n, FockScratch sc, double fp, double jp,
-                                                               double kp, int zero_f) {
+__global__ void __launch_bounds__(128) k_fock_combine(double *F, int n, FockScratch sc, double fp, double jp,
+                                                      double kp, int zero_f) {
     const int i = blockIdx.x;
-    for (int j = threadIdx.x; j < n; j += kFockThreads) {
+    for (int j = threadIdx.x; j < n; j += 128) {
         const double yj = sc.YJ[(size_t)max(i, j) * n + min(i, j)];
         const double J = (i == j ? 4.0 : 2.0) * yj;
         const double K = sc.XK[(size_t)i * n + j] + sc.XK[(size_t)j * n + i];
@@ -241,66 +482,99 @@ __global__ void __launch_bounds__(kFockThreads) k_fock_combine(double *F, int n,
     }
 }
 
+template <int S>
+eg_status launch_lines(const double *g, const double *D, int n, const FockScratch &sc, cudaStream_t s) {
+    int units = 0;
+    for (int p = 0; p < n; p++) units += (p + kWarps) / kWarps;
+    const unsigned chunks = (unsigned)((n + 31) / 32);
+    if constexpr (S > 0) {
+        {
+            LaunchScope ls_("k_fock_digits_d", s);
+            k_fock_digits_d<S><<<n, 128, 0, s>>>(D, n, (float *)sc.Dd, (int *)sc.De);
+        }
+        EG_CHECK_LAUNCH("k_fock_digits_d");
+    }
+    {
+        LaunchScope ls_("k_fock_rows", s);
+        k_fock_rows<S><<<dim3((unsigned)units, chunks), kWarps * 32, 0, s>>>(g, D, n, sc);
+    }
+    EG_CHECK_LAUNCH("k_fock_rows");
+    {
+        LaunchScope ls_("k_fock_cols", s);
+        k_fock_cols<S><<<dim3((unsigned)units, chunks), kWarps * 32, 0, s>>>(g, D, n, sc);
+    }
+    EG_CHECK_LAUNCH("k_fock_cols");
+    return EG_SUCCESS;
+}
+
 } // namespace
 
 } // namespace eg
 
 extern "C" eg_status eg_fock_jk_symmetric(double F_prefactor, double *F, double J_prefactor, double K_prefactor,
-                                          const double *g, const double *D, int64_t n, void *stream) {
+                                          const double *g, const double *D, int64_t n, const eg_options *opt,
+                                          void *stream) {
     using namespace eg;
     set_error("");
+    eg_options o;
+    eg_options_default(&o);
+    if (opt) o = *opt;
+    if (o.precision != EG_PRECISION_FP64 && o.precision != EG_PRECISION_SPLIT_BF16)
+        return fail(EG_ERROR_INVALID_ARGUMENT, "eg_fock_jk_symmetric: unknown precision");
+    const int S = o.precision == EG_PRECISION_SPLIT_BF16 ? (o.slices ? o.slices : 5) : 0;
+    if (S != 0 && (S < 3 || S > 6))
+        return fail(EG_ERROR_INVALID_ARGUMENT, "eg_fock_jk_symmetric: slices must be in 3..6");
     if (n < 0) return fail(EG_ERROR_INVALID_ARGUMENT, "eg_fock_jk_symmetric: negative n");
     if (n == 0) return EG_SUCCESS;
     if (!F || !g || !D) return fail(EG_ERROR_INVALID_ARGUMENT, "eg_fock_jk_symmetric: NULL pointer");
-    // pair-block shared memory: 64 staged rows of up to n doubles plus two rows of D
-    const size_t smem = ((size_t)kFockChunk * (size_t)(n | 1) + 2 * (size_t)n) * sizeof(double);
-    if (n > 46340 / 2 || smem > 220 * 1024)
+    if (n > kFockMaxN)
         return fail(EG_ERROR_NOT_SUPPORTED, "eg_fock_jk_symmetric: n = " + std::to_string(n) +
-                                                " exceeds the largest supported (" +
-                                                std::to_string((220 * 1024 / 8 - 0) / (kFockChunk + 2)) + ")");
+                                                " exceeds the largest supported (" + std::to_string(kFockMaxN) + ")");
     const int nn = (int)n;
-    const int nc = (nn + kFockChunk - 1) / kFockChunk;
-    const size_t n3 = (size_t)nn * nn * nn;
-    const size_t elems = 2 * n3 + 2 * n3 * nc + (size_t)nn * nn * nc + 3 * (size_t)nn * nn;
+    const int nsc = (nn + 31) / 32;
+    const size_t n3 = (size_t)nn * nn * nn, n2 = (size_t)nn * nn;
+    const size_t elems = 4 * n3 + n2 * nsc + n2 * kExPSplit + 2 * n2;
+    const size_t dd_bytes = S ? (n2 * S * sizeof(float) + (size_t)nn * sizeof(int) + 256) : 0;
     cudaStream_t s = (cudaStream_t)stream;
     void *ws = nullptr;
-    eg_status st = workspace(s, elems * sizeof(double), &ws);
+    eg_status st = workspace(s, elems * sizeof(double) + dd_bytes, &ws);
     if (st != EG_SUCCESS) return st;
     FockScratch sc;
     sc.S1 = (double *)ws;
     sc.S4 = sc.S1 + n3;
     sc.S2 = sc.S4 + n3;
-    sc.S5 = sc.S2 + n3 * nc;
-    sc.X3 = sc.S5 + n3 * nc;
-    sc.X6 = sc.X3 + (size_t)nn * nn * nc;
-    sc.YJ = sc.X6 + (size_t)nn * nn;
-    sc.XK = sc.YJ + (size_t)nn * nn;
-    static bool attr_set = false;
-    if (!attr_set) {
-        EG_CUDA(cudaFuncSetAttribute(k_fock_pair_blocks, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
-        attr_set = true;
+    sc.S5 = sc.S2 + n3;
+    sc.X3 = sc.S5 + n3;
+    sc.X6 = sc.X3 + n2 * nsc;
+    sc.YJ = sc.X6 + n2 * kExPSplit;
+    sc.XK = sc.YJ + n2;
+    sc.Dd = S ? (const float *)(sc.XK + n2) : nullptr;
+    sc.De = S ? (const int *)(sc.Dd + n2 * S) : nullptr;
+    sc.nsc = nsc;
+    switch (S) {
+    case 0: st = launch_lines<0>(g, D, nn, sc, s); break;
+    case 3: st = launch_lines<3>(g, D, nn, sc, s); break;
+    case 4: st = launch_lines<4>(g, D, nn, sc, s); break;
+    case 5: st = launch_lines<5>(g, D, nn, sc, s); break;
+    default: st = launch_lines<6>(g, D, nn, sc, s); break;
     }
+    if (st != EG_SUCCESS) return st;
     {
-        LaunchScope ls_("k_fock_pair_blocks", s);
-        k_fock_pair_blocks<<<dim3((unsigned)(nn * (nn + 1) / 2), (unsigned)nc), kFockThreads, smem, s>>>(g, D, nn, nc,
-                                                                                                        sc);
+        LaunchScope ls_("k_fock_exchange", s);
+        k_fock_exchange<<<dim3((unsigned)(nn * nsc), kExPSplit), kWarps * 32, 0, s>>>(g, D, nn, nsc, sc.X6);
     }
-    EG_CHECK_LAUNCH("k_fock_pair_blocks");
-    {
-        LaunchScope ls_("k_fock_exchange_blocks", s);
-        k_fock_exchange_blocks<<<(unsigned)(nn * nn), kFockThreads, 0, s>>>(g, D, nn, sc.X6);
-    }
-    EG_CHECK_LAUNCH("k_fock_exchange_blocks");
+    EG_CHECK_LAUNCH("k_fock_exchange");
     {
         LaunchScope ls_("k_fock_reduce", s);
-        k_fock_reduce<<<(unsigned)nn, kFockThreads, 0, s>>>(nn, nc, sc);
+        k_fock_reduce<<<dim3((unsigned)nn, (unsigned)nsc), kRedWarps * 32, 0, s>>>(nn, sc);
     }
     EG_CHECK_LAUNCH("k_fock_reduce");
     {
         LaunchScope ls_("k_fock_combine", s);
-        k_fock_combine<<<(unsigned)nn, kFockThreads, 0, s>>>(F, nn, sc, F_prefactor, J_prefactor, K_prefactor,
-                                                            F_prefactor == 0.0 ? 1 : 0);
+        k_fock_combine<<<(unsigned)nn, 128, 0, s>>>(F, nn, sc, F_prefactor, J_prefactor, K_prefactor,
+                                                   F_prefactor == 0.0 ? 1 : 0);
     }
     EG_CHECK_LAUNCH("k_fock_combine");
+    if (S) set_split_report(eg_split_report{S, S * (S + 1) / 2, split::kBits, split::error_bound(S)});
     return EG_SUCCESS;
 }

@@ -20,6 +20,8 @@
 #include "common.cuh"
 
 namespace eg {
+eg_status build_permute_desc(double cp, const int32_t *Cl, const eg_tensor *C, double ap, const int32_t *Al,
+                             const eg_tensor *A, PermuteDesc &p);
 
 namespace {
 
@@ -138,7 +140,23 @@ __global__ void __launch_bounds__(TILE *ROWS) k_permute_tiles(PermuteMap rest, i
 
 } // namespace
 
-eg_status launch_permute(const PermuteDesc &p, cudaStream_t s) {
+// What a permute launch needs, fixed by the shapes and strides alone: a
+// compiled plan keeps it and runs it on new pointers.
+struct PermuteLaunch {
+    bool empty = false;
+    bool rows = false; // fastest modes shared: row copies, else tiles
+    int mode = 0;      // 0: copy, 1: ap*a, 2: ap*a + cp*c
+    int grid = 0;
+    PermuteMap rest;
+    int64_t L = 0, sa = 0, sc = 0;                                 // rows
+    int64_t EA = 0, EC = 0, saA = 0, scA = 0, saC = 0, scC = 0; // tiles
+    double ap = 1.0, cp = 0.0;
+};
+
+PermuteLaunch prepare_permute(const PermuteDesc &p) {
+    PermuteLaunch pl;
+    pl.ap = p.ap;
+    pl.cp = p.cp;
     // Fold modes (in C order) that are contiguous in both tensors; drop extent-1 modes.
     std::vector<int64_t> ext, sA, sC;
     int64_t total = 1;
@@ -155,7 +173,10 @@ eg_status launch_permute(const PermuteDesc &p, cudaStream_t s) {
         sA.push_back(p.sA[d]);
         sC.push_back(p.sC[d]);
     }
-    if (total == 0) return EG_SUCCESS;
+    if (total == 0) {
+        pl.empty = true;
+        return pl;
+    }
     if (ext.empty()) { // a single element
         ext.push_back(1);
         sA.push_back(1);
@@ -169,55 +190,105 @@ eg_status launch_permute(const PermuteDesc &p, cudaStream_t s) {
         return best;
     };
     const int fa = argmin(sA), fc = argmin(sC);
-    const int mode = (p.cp == 0.0) ? (p.ap == 1.0 ? 0 : 1) : 2;
+    pl.mode = (p.cp == 0.0) ? (p.ap == 1.0 ? 0 : 1) : 2;
     const int cap = num_sms() * 16;
-
-    PermuteMap rest;
     for (int d = 0; d < n; d++) {
         if (d == fa || d == fc) continue;
-        rest.ext[rest.n] = ext[d];
-        rest.sA[rest.n] = sA[d];
-        rest.sC[rest.n] = sC[d];
-        rest.total *= ext[d];
-        rest.n++;
+        pl.rest.ext[pl.rest.n] = ext[d];
+        pl.rest.sA[pl.rest.n] = sA[d];
+        pl.rest.sC[pl.rest.n] = sC[d];
+        pl.rest.total *= ext[d];
+        pl.rest.n++;
     }
     if (fa == fc) {
-        const int64_t L = ext[fc];
-        const int64_t work = (rest.total * ((L + kRowChunk - 1) / kRowChunk) + 7) / 8;
-        const int grid = (int)(work < cap ? work : cap);
-        if (mode == 0)
-            { LaunchScope ls_("k_permute_rows", s);
-            k_permute_rows<0><<<grid, 256, 0, s>>>(rest, L, sA[fc], sC[fc], p.A, p.C, p.ap, p.cp);
-            }
-        else if (mode == 1)
-            { LaunchScope ls_("k_permute_rows", s);
-            k_permute_rows<1><<<grid, 256, 0, s>>>(rest, L, sA[fc], sC[fc], p.A, p.C, p.ap, p.cp);
-            }
-        else
-            { LaunchScope ls_("k_permute_rows", s);
-            k_permute_rows<2><<<grid, 256, 0, s>>>(rest, L, sA[fc], sC[fc], p.A, p.C, p.ap, p.cp);
-            }
+        pl.rows = true;
+        pl.L = ext[fc];
+        pl.sa = sA[fc];
+        pl.sc = sC[fc];
+        const int64_t work = (pl.rest.total * ((pl.L + kRowChunk - 1) / kRowChunk) + 7) / 8;
+        pl.grid = (int)(work < cap ? work : cap);
+        return pl;
+    }
+    pl.EA = ext[fa];
+    pl.EC = ext[fc];
+    pl.saA = sA[fa];
+    pl.scA = sC[fa];
+    pl.saC = sA[fc];
+    pl.scC = sC[fc];
+    const int64_t work =
+        pl.rest.total * ((pl.EA + TILE - 1) / TILE) * (((pl.EC + TILE - 1) / TILE + kStrip - 1) / kStrip);
+    pl.grid = (int)(work < cap ? work : cap);
+    return pl;
+}
+
+eg_status run_permute(const PermuteLaunch &pl, const double *A, double *C, cudaStream_t s) {
+    if (pl.empty) return EG_SUCCESS;
+    if (pl.rows) {
+        {
+            LaunchScope ls_("k_permute_rows", s);
+            if (pl.mode == 0)
+                k_permute_rows<0><<<pl.grid, 256, 0, s>>>(pl.rest, pl.L, pl.sa, pl.sc, A, C, pl.ap, pl.cp);
+            else if (pl.mode == 1)
+                k_permute_rows<1><<<pl.grid, 256, 0, s>>>(pl.rest, pl.L, pl.sa, pl.sc, A, C, pl.ap, pl.cp);
+            else
+                k_permute_rows<2><<<pl.grid, 256, 0, s>>>(pl.rest, pl.L, pl.sa, pl.sc, A, C, pl.ap, pl.cp);
+        }
         EG_CHECK_LAUNCH("k_permute_rows");
         return EG_SUCCESS;
     }
-    const int64_t EA = ext[fa], EC = ext[fc];
-    const int64_t work = rest.total * ((EA + TILE - 1) / TILE) * (((EC + TILE - 1) / TILE + kStrip - 1) / kStrip);
-    const int grid = (int)(work < cap ? work : cap);
-    dim3 block(TILE, ROWS);
-    if (mode == 0)
-        { LaunchScope ls_("k_permute_tiles", s);
-        k_permute_tiles<0><<<grid, block, 0, s>>>(rest, EA, EC, sA[fa], sC[fa], sA[fc], sC[fc], p.A, p.C, p.ap, p.cp);
-        }
-    else if (mode == 1)
-        { LaunchScope ls_("k_permute_tiles", s);
-        k_permute_tiles<1><<<grid, block, 0, s>>>(rest, EA, EC, sA[fa], sC[fa], sA[fc], sC[fc], p.A, p.C, p.ap, p.cp);
-        }
-    else
-        { LaunchScope ls_("k_permute_tiles", s);
-        k_permute_tiles<2><<<grid, block, 0, s>>>(rest, EA, EC, sA[fa], sC[fa], sA[fc], sC[fc], p.A, p.C, p.ap, p.cp);
-        }
+    const dim3 block(TILE, ROWS);
+    {
+        LaunchScope ls_("k_permute_tiles", s);
+        if (pl.mode == 0)
+            k_permute_tiles<0><<<pl.grid, block, 0, s>>>(pl.rest, pl.EA, pl.EC, pl.saA, pl.scA, pl.saC, pl.scC, A, C,
+                                                        pl.ap, pl.cp);
+        else if (pl.mode == 1)
+            k_permute_tiles<1><<<pl.grid, block, 0, s>>>(pl.rest, pl.EA, pl.EC, pl.saA, pl.scA, pl.saC, pl.scC, A, C,
+                                                        pl.ap, pl.cp);
+        else
+            k_permute_tiles<2><<<pl.grid, block, 0, s>>>(pl.rest, pl.EA, pl.EC, pl.saA, pl.scA, pl.saC, pl.scC, A, C,
+                                                        pl.ap, pl.cp);
+    }
     EG_CHECK_LAUNCH("k_permute_tiles");
     return EG_SUCCESS;
 }
 
+eg_status launch_permute(const PermuteDesc &p, cudaStream_t s) { return run_permute(prepare_permute(p), p.A, p.C, s); }
+
 } // namespace eg
+
+struct eg_permute_plan {
+    eg::PermuteLaunch launch;
+};
+
+extern "C" {
+
+eg_status eg_permute_plan_create(double C_prefactor, const int32_t *C_labels, const eg_tensor *C, double A_prefactor,
+                                 const int32_t *A_labels, const eg_tensor *A, eg_permute_plan **plan) {
+    eg::set_error("");
+    if (!plan) return eg::fail(EG_ERROR_INVALID_ARGUMENT, "plan is NULL");
+    *plan = nullptr;
+    try {
+        eg::PermuteDesc d;
+        const eg_status st = eg::build_permute_desc(C_prefactor, C_labels, C, A_prefactor, A_labels, A, d);
+        if (st != EG_SUCCESS) return st;
+        *plan = new eg_permute_plan{eg::prepare_permute(d)};
+        return EG_SUCCESS;
+    } catch (...) {
+        return eg::fail(EG_ERROR_OUT_OF_MEMORY, "eg_permute_plan_create: allocation failed");
+    }
+}
+
+eg_status eg_permute_plan_execute(const eg_permute_plan *plan, double *C, const double *A, void *stream) {
+    eg::set_error("");
+    if (!plan) return eg::fail(EG_ERROR_INVALID_ARGUMENT, "plan is NULL");
+    if (!plan->launch.empty && (!C || !A)) return eg::fail(EG_ERROR_INVALID_ARGUMENT, "C or A is NULL");
+    return eg::run_permute(plan->launch, A, C, (cudaStream_t)stream);
+}
+
+eg_status eg_permute_plan_destroy(eg_permute_plan *plan) {
+    delete plan;
+    return EG_SUCCESS;
+}
+
+} // extern "C"

@@ -148,38 +148,6 @@ __device__ __forceinline__ int entry_nkb(const TcGemmParams &p, const TcItem *it
     return min(p.kslice, p.nkb - kbeg);
 }
 
-__device__ __forceinline__ double scale_pow2(double v, int e) {
-    if (v == 0.0) return v;
-    const long long bits = __double_as_longlong(v);
-    const int ex = (int)((bits >> 52) & 0x7ff);
-    const int ne = ex + e;
-    if (ex != 0 && ne > 0 && ne < 2047) return __longlong_as_double(bits + ((long long)e << 52));
-    return scalbn(v, e);
-}
-
-// R * 2^e rounded to nearest (ties to even), built with integer operations so
-// the FP64 pipe -- about 1.75 operations per clock per SM on this GPU -- is
-// left for the one fused multiply-add with C.  Falls back to the FP64 path
-// when the result would not be a normal number.
-__device__ __forceinline__ double int64_times_pow2(long long R, int e) {
-    if (R == 0) return 0.0;
-    const unsigned long long sign = R < 0 ? 0x8000000000000000ull : 0ull;
-    const unsigned long long a = R < 0 ? (unsigned long long)(-R) : (unsigned long long)R;
-    const int lz = __clzll((long long)a);
-    const unsigned long long x = a << lz;      // leading one at bit 63
-    unsigned long long mant = x >> 11;         // 53 bits, leading one at bit 52
-    const unsigned long long rem = x & 0x7FFull;
-    if (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) mant++;
-    int exp = 63 - lz + e;
-    if (mant >> 53) {
-        mant >>= 1;
-        exp++;
-    }
-    const int biased = exp + 1023;
-    if (biased <= 0 || biased >= 2047) return scale_pow2(__ll2double_rn(R), e);
-    return __longlong_as_double((long long)(sign | ((unsigned long long)biased << 52) | (mant & 0xFFFFFFFFFFFFFull)));
-}
-
 // Issues the 4 * NB MMAs of one group (K blocks at A/B descriptors a0, b0;
 // a second block sits A_BYTES / B_BYTES further on) and, in the same
 // instruction sequence, tests whether phase `parity` of the barrier at
@@ -475,7 +443,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             if (pend_rowExp == INT_MIN || ce == INT_MIN)
                                 v = __longlong_as_double(0x7ff8000000000000ll);
                             else
-                                v = int64_times_pow2(R, pend_rowExp + ce + p.shift_const);
+                                v = int_times_pow2_rn(R, pend_rowExp + ce + p.shift_const);
                             if (!p.ab_pow2) v *= p.ab;
                             pend_C[rowOff + colOff[c0 + i]] =
                                 plain_store ? v : (cp_one ? old[i] + v : fma(p.cp, old[i], v));
@@ -512,7 +480,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                             if (pend_rowExp == INT_MIN || ce == INT_MIN)
                                 v = __longlong_as_double(0x7ff8000000000000ll);
                             else
-                                v = int64_times_pow2(R, pend_rowExp + ce + p.shift_const);
+                                v = int_times_pow2_rn(R, pend_rowExp + ce + p.shift_const);
                             if (!p.ab_pow2) v *= p.ab;
                         }
                         finT[i * FIN_T + lane] = v;
@@ -698,7 +666,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                                 if (rowExp == INT_MIN || ce == INT_MIN)
                                     v[i] = __longlong_as_double(0x7ff8000000000000ll);
                                 else
-                                    v[i] = int64_times_pow2(R, rowExp + ce + p.shift_const);
+                                    v[i] = int_times_pow2_rn(R, rowExp + ce + p.shift_const);
                                 if (!p.ab_pow2) v[i] *= p.ab;
                             }
                         }

@@ -121,6 +121,21 @@ eg_status eg_permute(double C_prefactor, const int32_t *C_labels, const eg_tenso
                      const int32_t *A_labels, const eg_tensor *A, void *stream);
 
 /*
+ * Compiled permute: the plan fixes the index permutation, the extents and strides of C and A
+ * and the prefactors (the data pointers in C and A are not kept); execute runs it on any C
+ * and A of those shapes and strides -- C = C_prefactor * C + A_prefactor * A[perm], as
+ * eg_permute.  Replaces compile_permute(beta, Indices{...}, &C, alpha, Indices{...}, A)
+ * (libs/Einsums/TensorAlgebra/include/Einsums/TensorAlgebra/Permute.hpp:37-171), which builds
+ * a reusable HPTT plan, and permute(&C, A, plan) (Permute.hpp:292-297), which rebinds the
+ * plan's input and output pointers and executes it.
+ */
+typedef struct eg_permute_plan eg_permute_plan;
+eg_status eg_permute_plan_create(double C_prefactor, const int32_t *C_labels, const eg_tensor *C, double A_prefactor,
+                                 const int32_t *A_labels, const eg_tensor *A, eg_permute_plan **plan);
+eg_status eg_permute_plan_execute(const eg_permute_plan *plan, double *C, const double *A, void *stream);
+eg_status eg_permute_plan_destroy(eg_permute_plan *plan);
+
+/*
  * List einsum: item i computes C[i] = C_prefactor*C[i] + AB_prefactor * A[i]*B[i] with one
  * shared index pattern.  Items may have different extents.  Lists of contractions run as a
  * grouped plan (see eg_grouped_plan_create), cached by call signature and replayed as a
@@ -173,16 +188,21 @@ eg_status eg_dot_noalloc(double C_prefactor, double *C, double AB_prefactor, con
  * g: n^4 contiguous row-major doubles with g[p,q,r,s] = g[q,p,r,s] = g[p,q,s,r] = g[r,s,p,q];
  * D and F: n x n contiguous row-major, D symmetric.  These symmetries are the caller's
  * contract and are not checked: only the canonical eighth of g (p >= q, r >= s,
- * pair(p,q) >= pair(r,s)) is read, and D[r,s] stands for D[s,r].  FP64 throughout, with a
- * deterministic summation order.  Replaces the pair of einsum calls of the reference's RHF
+ * pair(p,q) >= pair(r,s)) is read, and D[r,s] stands for D[s,r].  opt (may be NULL): precision
+ * EG_PRECISION_FP64 (default) makes all six contributions of each element in FP64;
+ * EG_PRECISION_SPLIT_BF16 cuts g and D into opt->slices (3..6, 0 = 5) 8-bit digits -- the
+ * digits of the split-BF16 contraction -- and sums four of the six contributions as exact
+ * digit products on the FP32 pipe, the other two in FP64 (error bound as
+ * eg_last_split_report states: 1.3e-11 for 5 slices).  The summation order is fixed, so the
+ * results are deterministic.  Replaces the pair of einsum calls of the reference's RHF
  * Fock build, F += 2 einsum(pq <- pqrs, rs) and F -= einsum(pq <- prqs, rs)
  * (libs/Einsums/TensorAlgebra/tests/unit/QChemTests.cpp:300-303; dispatch
  * Backends/Dispatch.hpp:444-560 and Backends/BaseAlgebra.hpp:85-139): J_prefactor = 2,
- * K_prefactor = -1, F_prefactor = 1.  EG_ERROR_NOT_SUPPORTED when n is too large for the
- * staged blocks (n above about 400).
+ * K_prefactor = -1, F_prefactor = 1.  EG_ERROR_NOT_SUPPORTED for n above 384 (g is then
+ * 174 GB).
  */
 eg_status eg_fock_jk_symmetric(double F_prefactor, double *F, double J_prefactor, double K_prefactor, const double *g,
-                               const double *D, int64_t n, void *stream);
+                               const double *D, int64_t n, const eg_options *opt, void *stream);
 
 /*
  * Grouped plan: lowers every item of a list einsum once, builds a device-side work list of

@@ -327,6 +327,44 @@ void permute(U const C_prefactor, std::tuple<CIndices...> const &C_indices, CTyp
         eg_permute((double)C_prefactor, cl.data(), &tc, (double)A_prefactor, al.data(), &ta, default_options().stream));
 }
 
+// compile_permute(beta, Cidx, &C, alpha, Aidx, A) (Permute.hpp:37-171): a reusable plan
+// for tensors of C's and A's shapes and strides; permute(&C, A, plan) runs it on new data
+// (Permute.hpp:292-297).
+class PermutePlan {
+  public:
+    explicit PermutePlan(eg_permute_plan *p) : p_(p) {}
+    PermutePlan(PermutePlan const &) = delete;
+    PermutePlan &operator=(PermutePlan const &) = delete;
+    PermutePlan(PermutePlan &&o) noexcept : p_(o.p_) { o.p_ = nullptr; }
+    ~PermutePlan() {
+        if (p_) eg_permute_plan_destroy(p_);
+    }
+    eg_permute_plan *get() const { return p_; }
+
+  private:
+    eg_permute_plan *p_;
+};
+
+template <typename AType, typename CType, typename U, typename... CIndices, typename... AIndices>
+std::shared_ptr<PermutePlan> compile_permute(U const C_prefactor, std::tuple<CIndices...> const &C_indices, CType *C,
+                                             U const A_prefactor, std::tuple<AIndices...> const &A_indices,
+                                             AType const &A) {
+    static_assert(sizeof...(CIndices) == sizeof...(AIndices), "permute needs the same number of indices");
+    static_assert(sizeof...(CIndices) == CType::rank && sizeof...(AIndices) == AType::rank, "rank mismatch");
+    const auto cl = detail::label_vector(C_indices), al = detail::label_vector(A_indices);
+    const eg_tensor tc = C->descriptor(), ta = A.descriptor();
+    eg_permute_plan *p = nullptr;
+    ::einsums::detail::check(
+        eg_permute_plan_create((double)C_prefactor, cl.data(), &tc, (double)A_prefactor, al.data(), &ta, &p));
+    return std::make_shared<PermutePlan>(p);
+}
+
+template <typename AType, typename CType>
+void permute(CType *C, AType const &A, std::shared_ptr<PermutePlan> const &plan) {
+    const eg_tensor tc = C->descriptor(), ta = A.descriptor();
+    ::einsums::detail::check(eg_permute_plan_execute(plan->get(), tc.data, ta.data, default_options().stream));
+}
+
 } // namespace tensor_algebra
 
 } // namespace einsums

@@ -143,6 +143,18 @@ int main() {
             threw = true;
         }
         CHECK(threw);
+        // a compiled plan reused on new data (compile_permute + permute(&C, A, plan))
+        auto plan = compile_permute(0.0, Indices{index::j, index::i}, &C, 1.0, Indices{index::i, index::j}, A);
+        for (int rep = 1; rep <= 2; rep++) {
+            for (int x = 0; x < 12; x++) h[x] = x * 10.0 * rep;
+            A.write(h);
+            permute(&C, A, plan);
+            got = C.read();
+            ok = true;
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 4; j++) ok &= got[j * 3 + i] == h[i * 4 + j];
+            CHECK(ok);
+        }
     }
     if (failures == 0) std::printf("frontend_test: all checks passed\n");
     return failures == 0 ? 0 : 1;

@@ -11,17 +11,16 @@ element g, scaled by its degeneracy f = 1/2 for each of p == q, r == s and
 pair(p,q) == pair(r,s), makes six contributions to two non-symmetric
 accumulators YJ and XK (J = 2 (YJ + YJ^T), K = XK + XK^T):
 
-    T1  YJ[p,q] += f g D[r,s]        row sums of a (p, r) block over s
-    T2  YJ[r,s] += f g D[p,q]        column sums over q
-    T3  XK[p,r] += f g D[q,s]        the block's weighted total
-    T4  XK[q,r] += f g D[p,s]        row sums over s
-    T5  XK[p,s] += f g D[q,r]        column sums over q
-    T6  XK[q,s] += f g D[p,r]        the weighted total of a (q, s) block
+    T1  YJ[p,q] += f g D[r,s]        rows pass: per (p, r, q), sum over s
+    T2  YJ[r,s] += f g D[p,q]        columns pass: per (p, r, s), sum over q
+    T3  XK[p,r] += f g D[q,s]        columns pass: per (p, r), sum over (q, s)
+    T4  XK[q,r] += f g D[p,s]        rows pass
+    T5  XK[p,s] += f g D[q,r]        columns pass
+    T6  XK[q,s] += f g D[p,r]        exchange pass: per (q, s), sum over (p, r)
 
-T1-T5 come from "pair blocks" B[q, s] = g[p, q, r, s] (p >= r; q <= p; s <= r,
-and s <= q when p == r); T6 from "exchange blocks" over (p, r) for fixed
-(q, s), read through g[p,q,r,s] = g[q,p,s,r].  The per-block vectors go to
-scratch and are summed in a fixed order by a final pass.
+The rows pass reads g[r,s,p,q] (= g[p,q,r,s]) and the exchange pass g[q,p,r,s]
+(= g[p,q,r,s]), so that each line's lanes read consecutive addresses; the
+per-line results go to scratch and a reduction adds them in a fixed order.
 """
 import numpy as np
 import pytest
@@ -39,46 +38,42 @@ def sym_inputs(n, seed):
 
 def fock_jk_restated(g, D):
     n = g.shape[0]
-    S1 = np.zeros((n, n, n))  # [p][r][q]  T1
-    S2 = np.zeros((n, n, n))  # [r][p][s]  T2
-    S4 = np.zeros((n, n, n))  # [r][p][q]  T4
-    S5 = np.zeros((n, n, n))  # [p][r][s]  T5
-    X3 = np.zeros((n, n))     # [p][r]     T3 (p >= r)
-    X6 = np.zeros((n, n))     # [q][s]     T6
+    S1 = np.zeros((n, n, n))  # [p][r][q]
+    S4 = np.zeros((n, n, n))  # [q][p][r]
+    S2 = np.zeros((n, n, n))  # [r][p][s]
+    S5 = np.zeros((n, n, n))  # [p][r][s]
+    X3 = np.zeros((n, n))     # [p][r]
+    X6 = np.zeros((n, n))     # [q][s]
+
+    def f(p, q, r, s):
+        return (0.5 if p == q else 1.0) * (0.5 if r == s else 1.0) * (0.5 if (p == r and q == s) else 1.0)
+
     for p in range(n):
         for r in range(p + 1):
-            B = np.zeros((p + 1, r + 1))
-            for q in range(p + 1):
-                smax = r if p > r else q
-                B[q, :smax + 1] = g[p, q, r, :smax + 1]
-            B = B.copy()
-            B[p, :] *= 0.5                 # p == q
-            B[:, r] *= 0.5                 # r == s
-            if p == r:
-                B[np.arange(p + 1), np.arange(p + 1)] *= 0.5   # pair(p,q) == pair(r,s)
-            S1[p, r, :p + 1] = B @ D[r, :r + 1]
-            S4[r, p, :p + 1] = B @ D[p, :r + 1]
-            S2[r, p, :r + 1] = D[p, :p + 1] @ B
-            S5[p, r, :r + 1] = D[:p + 1, r] @ B
-            X3[p, r] = np.sum(B * D[:p + 1, :r + 1])
-    for q in range(n):
+            for q in range(p + 1):  # rows pass: line (p, r, q) over s, read as g[r,s,p,q]
+                for s in range(r + 1 if p > r else q + 1):
+                    v = f(p, q, r, s) * g[r, s, p, q]
+                    S1[p, r, q] += v * D[r, s]
+                    S4[q, p, r] += v * D[p, s]
+            for s in range(r + 1):  # columns pass: line (p, r, s) over q
+                for q in range(s if p == r else 0, p + 1):
+                    v = f(p, q, r, s) * g[p, q, r, s]
+                    S2[r, p, s] += v * D[p, q]
+                    S5[p, r, s] += v * D[q, r]
+                    X3[p, r] += v * D[q, s]
+    for q in range(n):  # exchange pass: (q, s) over p >= q, s <= r <= p (r < p when q < s), read as g[q,p,r,s]
         for s in range(n):
-            acc = 0.0
-            for p in range(q, n):
-                for rr in range(s, n):
-                    if not (p > rr or (p == rr and q >= s)):
-                        continue
-                    f = (0.5 if p == q else 1.0) * (0.5 if rr == s else 1.0) * (0.5 if (p == rr and q == s) else 1.0)
-                    acc += f * g[q, p, s, rr] * D[p, rr]
-            X6[q, s] = acc
+            for p in range(max(q, s), n):
+                for r in range(s, (p - 1 if q < s else p) + 1):
+                    X6[q, s] += f(p, q, r, s) * g[q, p, r, s] * D[p, r]
     YJ = np.zeros((n, n))
     XK = X6.copy()
     for i in range(n):
         for j in range(n):
+            XK[i, j] += sum(S4[i, p, j] for p in range(max(i, j), n))
             if i >= j:
-                YJ[i, j] = sum(S1[i, r, j] for r in range(i + 1)) + sum(S2[i, p, j] for p in range(i, n))
                 XK[i, j] += X3[i, j] + sum(S5[i, r, j] for r in range(j, i + 1))
-            XK[i, j] += sum(S4[j, p, i] for p in range(max(i, j), n))
+                YJ[i, j] = sum(S1[i, r, j] for r in range(i + 1)) + sum(S2[i, p, j] for p in range(i, n))
     return 2.0 * (YJ + YJ.T), XK + XK.T
 
 

@@ -157,8 +157,8 @@ def test_device_digit_arithmetic_matches_the_definition(S):
             assert _digits_dev(float(X[i, j]), int(e[i]), S) == [int(D[s, i, j]) for s in range(S)]
 
 
-def _int64_times_pow2_dev(R, e):
-    """int64_times_pow2 of the tensor kernel's epilogue: R * 2^e rounded to nearest
+def _int_times_pow2_rn_dev(R, e):
+    """int_times_pow2_rn of split.cuh (the tensor kernel's epilogue): R * 2^e rounded to nearest
     even, built on the IEEE fields (leading-zero count, 53-bit mantissa with
     half-even rounding of the 11 dropped bits); None where the kernel leaves the
     result to its FP64 fallback (exponent out of the normal range)."""
@@ -190,7 +190,7 @@ def test_epilogue_int64_to_double_rounds_half_even():
     cases += [int(v) << int(s) for v, s in zip(rng.integers(-2 ** 20, 2 ** 20, size=100), rng.integers(0, 40, size=100))]
     for R in cases:
         for e in (-1074 + 64, -200, -46, 0, 17, 900):
-            got = _int64_times_pow2_dev(R, e)
+            got = _int_times_pow2_rn_dev(R, e)
             if got is None:
                 continue  # out of the normal range: the kernel's FP64 fallback handles it
             assert got == math.ldexp(float(R), e), (R, e)  # float(int) rounds half to even
