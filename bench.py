@@ -292,8 +292,8 @@ def run_ours(args, rank, world):
 
     # FP64 roofline denominator, measured on this device.
     import ctypes
-    dfma, dmma = ctypes.c_double(), ctypes.c_double()
-    _lib.check(lib.eg_measure_fp64_peak(ctypes.byref(dfma), ctypes.byref(dmma)))
+    dfma, dmma, probe_mhz = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _lib.check(lib.eg_measure_fp64_peak_clock(ctypes.byref(dfma), ctypes.byref(dmma), ctypes.byref(probe_mhz)))
     fp64_peak = max(dfma.value, dmma.value)
 
     T = workloads.ccd_inputs(o, v, seed=args.seed, backend="cuda")
@@ -449,7 +449,8 @@ def run_ours(args, rank, world):
                        "l2": "inputs larger than L2 (Wabef 5.24 GB read+written per step); no flush",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "plain_fp64": {"value": fp64_value, "ms_per_step": ms_fp64, "per_contraction_ms": per_contraction_fp64,
-                           "fp64_peak_tflops": fp64_peak, "dfma_tflops": dfma.value, "dmma_tflops": dmma.value},
+                           "fp64_peak_tflops": fp64_peak, "dfma_tflops": dfma.value, "dmma_tflops": dmma.value,
+                           "fp64_probe_sm_mhz": probe_mhz.value},
             "split_vs_fp64_speedup": value / world / fp64_value if headline == "split_bf16" else None,
             "per_contraction_ms": per_contraction, "kernels": kernels, "kernels_steps": args.steps + args.warmup,
             "error_vs_fp64": errors, "error_fp64_vs_oracle_sample": oracle_err, "split_report": split_report,

@@ -83,6 +83,8 @@ PROTOTYPES = {
     "eg_permute_plan_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "eg_einsum_batched": (ctypes.c_int, [ctypes.c_double, _i32p, _T, ctypes.c_double, _i32p, _T, _i32p, _T,
                                          ctypes.c_int64, _P(EgOptions), ctypes.c_void_p, _i32p]),
+    "eg_einsum_complex": (ctypes.c_int, [_P(ctypes.c_double), _i32p, _T, _P(ctypes.c_double), _i32p, _T, _i32p,
+                                         _T, ctypes.c_int32, ctypes.c_int32, _P(EgOptions), ctypes.c_void_p, _i32p]),
     "eg_einsum_blocks": (ctypes.c_int, [ctypes.c_double, _i32p, _T, ctypes.c_double, _i32p, _T, _i32p, _T,
                                         ctypes.c_int64, _P(EgOptions), ctypes.c_void_p, _i32p]),
     "eg_dot_noalloc": (ctypes.c_int, [ctypes.c_double, ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p,
@@ -105,6 +107,7 @@ PROTOTYPES = {
     "eg_stream_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
     "eg_stream_status": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_int32)]),
     "eg_measure_fp64_peak": (ctypes.c_int, [_P(ctypes.c_double), _P(ctypes.c_double)]),
+    "eg_measure_fp64_peak_clock": (ctypes.c_int, [_P(ctypes.c_double), _P(ctypes.c_double), _P(ctypes.c_double)]),
     "eg_kernel_launches": (ctypes.c_int, [_P(ctypes.c_uint64)]),
     "eg_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_void_p]),
     "eg_profile_enable": (ctypes.c_int, [ctypes.c_int32]),

@@ -27,11 +27,11 @@ from ._lib import (PRECISION_FP64, PRECISION_SPLIT_BF16, SEMANTICS_CPP, SEMANTIC
 ALGORITHMS = ["GENERIC", "DOT", "DIRECT", "GER", "GEMV", "GEMM", "INDETERMINATE"]
 
 
-def _tensor(t: torch.Tensor, name: str) -> EgTensor:
+def _tensor(t: torch.Tensor, name: str, complex_ok: bool = False) -> EgTensor:
     if not isinstance(t, torch.Tensor):
         raise TypeError(f"{name} must be a torch.Tensor")
-    if t.dtype != torch.float64:
-        raise TypeError(f"{name} must be float64 (got {t.dtype})")
+    if t.dtype != torch.float64 and not (complex_ok and t.dtype == torch.complex128):
+        raise TypeError(f"{name} must be float64{' or complex128' if complex_ok else ''} (got {t.dtype})")
     if not t.is_cuda:
         raise TypeError(f"{name} must live on a CUDA device")
     if t.dim() > _lib.MAX_RANK:
@@ -74,11 +74,26 @@ def _check_device(*ts):
 
 
 def _run_einsum(C_prefactor, C_labels, C, AB_prefactor, A_labels, A, B_labels, B, *, semantics, precision="fp64",
-                slices=0, tolerance=1e-10, only_generic=False, stream=None) -> int:
+                slices=0, tolerance=1e-10, only_generic=False, stream=None, conj_A=False, conj_B=False) -> int:
     lib = _lib.load()
     if C.dim() != len(C_labels) or A.dim() != len(A_labels) or B.dim() != len(B_labels):
         raise _lib.RankError(2, "tensor ranks do not match the indices")
     _check_device(C, A, B)
+    if any(t.dtype == torch.complex128 for t in (C, A, B)):
+        if not all(t.dtype == torch.complex128 for t in (C, A, B)):
+            raise TypeError("complex einsum: C, A and B must all be complex128")
+        ec, ea, eb = _tensor(C, "C", True), _tensor(A, "A", True), _tensor(B, "B", True)
+        opt = _options(precision, slices, semantics, only_generic, tolerance)
+        alg = ctypes.c_int32(-1)
+        cpf, abf = complex(C_prefactor), complex(AB_prefactor)
+        cpa, aba = (ctypes.c_double * 2)(cpf.real, cpf.imag), (ctypes.c_double * 2)(abf.real, abf.imag)
+        _lib.check(lib.eg_einsum_complex(cpa, _lib.labels(C_labels), ctypes.byref(ec), aba, _lib.labels(A_labels),
+                                         ctypes.byref(ea), _lib.labels(B_labels), ctypes.byref(eb), int(bool(conj_A)),
+                                         int(bool(conj_B)), ctypes.byref(opt), ctypes.c_void_p(_stream(stream)),
+                                         ctypes.byref(alg)))
+        return alg.value
+    if conj_A or conj_B:
+        pass  # conjugating a real operand changes nothing (the reference's ConjA/ConjB on real data)
     ec, ea, eb = _tensor(C, "C"), _tensor(A, "A"), _tensor(B, "B")
     opt = _options(precision, slices, semantics, only_generic, tolerance)
     alg = ctypes.c_int32(-1)
@@ -291,7 +306,7 @@ def compile_plan(C_indices: str, A_indices: str, B_indices: str) -> EinsumGeneri
 # ------------------------------------------------------ C++-style calls ----
 def einsum(C_prefactor, C_indices: Sequence, C, AB_prefactor, A_indices: Sequence, A, B_indices: Sequence, B, *,
            precision: str = "fp64", slices: int = 0, tolerance: float = 1e-10, only_generic: bool = False,
-           stream=None) -> str:
+           stream=None, conj_A: bool = False, conj_B: bool = False) -> str:
     """C++-semantics einsum; returns the reference's AlgorithmChoice name.  C, A, B may also
     be equal-length lists (the batched overload), or BlockTensor / TiledTensor operands
     (blocks.py: every tile combination through one block-sparse call)."""
@@ -306,7 +321,7 @@ def einsum(C_prefactor, C_indices: Sequence, C, AB_prefactor, A_indices: Sequenc
         return ALGORITHMS[alg] if alg >= 0 else "INDETERMINATE"
     alg = _run_einsum(C_prefactor, list(C_indices), C, AB_prefactor, list(A_indices), A, list(B_indices), B,
                       semantics=SEMANTICS_CPP, precision=precision, slices=slices, tolerance=tolerance,
-                      only_generic=only_generic, stream=stream)
+                      only_generic=only_generic, stream=stream, conj_A=conj_A, conj_B=conj_B)
     return ALGORITHMS[alg]
 
 

@@ -283,6 +283,27 @@ eg_status classify_labels(const int32_t *Cl, int cr, const int32_t *Al, int ar, 
 
 } // namespace
 
+// The algorithm the reference reports for a call (classification and stride
+// vetoes), without running it.
+eg_status classify_call(const int32_t *Cl, const eg_tensor *C, const int32_t *Al, const eg_tensor *A,
+                        const int32_t *Bl, const eg_tensor *B, const eg_options *opt_in, int32_t *alg_out) {
+    eg_options opt;
+    eg_options_default(&opt);
+    if (opt_in) opt = *opt_in;
+    eg_status st;
+    if ((st = check_tensor(C, Cl, "C")) != EG_SUCCESS) return st;
+    if ((st = check_tensor(A, Al, "A")) != EG_SUCCESS) return st;
+    if ((st = check_tensor(B, Bl, "B")) != EG_SUCCESS) return st;
+    Algorithm alg;
+    classify_labels(Cl, C->rank, Al, A->rank, Bl, B->rank, opt.semantics, alg);
+    if (opt.only_generic) alg = Algorithm::GENERIC;
+    if (opt.semantics == EG_SEMANTICS_CPP)
+        alg = detail::apply_vetoes(alg, labels_of(Cl, C->rank), view_of(C), labels_of(Al, A->rank), view_of(A),
+                                   labels_of(Bl, B->rank), view_of(B));
+    *alg_out = (int32_t)alg;
+    return EG_SUCCESS;
+}
+
 eg_status einsum_impl(double cp, const int32_t *Cl, const eg_tensor *C, double ab, const int32_t *Al, const eg_tensor *A,
                       const int32_t *Bl, const eg_tensor *B, const eg_options *opt_in, cudaStream_t stream,
                       int32_t *alg_out) {

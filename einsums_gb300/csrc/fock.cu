@@ -35,13 +35,13 @@
 // shared-memory tiles, no atomics.  Every partial has one home and the last
 // passes add them in a fixed order, so the result is deterministic.
 //   k_fock_digits_d   (split form) the digits of every row of D.
-//   k_fock_rows<S>    warp (p, r, 32 q): T1 and T4, sums over s of
-//                     g[r,s,p,q] (= g[p,q,r,s]), lanes along q.
-//   k_fock_cols<S>    warp (p, r, 32 s): T2, T5 and T3, sums over q of
-//                     g[p,q,r,s], lanes along s.
-//   k_fock_exchange   CTA (q, 32 s, quarter of p): T6, sums over (p, r) of
-//                     g[q,p,r,s] (= g[p,q,r,s]) D[p,r], lanes along s.
-//   k_fock_reduce     one CTA per output row: YJ and XK from the partials.
+//   k_fock_rows<S>    unit r, a lane per pair (p, q): T1 and T4, sums over s
+//                     of g[r,s,p,q] (= g[p,q,r,s]), consecutive lanes along q.
+//   k_fock_cols<S>    unit p, a lane per pair (r, s): T2, T5 and T3, sums over
+//                     q of g[p,q,r,s], consecutive lanes along s.
+//   k_fock_exchange   warp (q, p, 32 s): T6, sums over r of g[q,p,r,s]
+//                     (= g[p,q,r,s]) D[p,r], lanes along s.
+//   k_fock_reduce     CTA (i, 32 j): YJ and XK from the partials.
 //   k_fock_combine    J = 2 (YJ + YJ^T), K = XK + XK^T and the prefactors.
 #include <algorithm>
 #include <climits>
@@ -58,17 +58,24 @@ using split::int_times_pow2_rn;
 using split::scaled_round;
 
 constexpr int kWarps = 4;      // warps per CTA of the line passes (consecutive r)
-constexpr int kExPSplit = 4;   // exchange CTAs over the p range of one (q, 32 s)
 constexpr int kRedWarps = 8;   // warps of a reduction CTA
 constexpr int kFockMaxN = 384; // g is 174 GB at n = 384
 constexpr int kFlush = 64;     // elements per exact FP32 digit-group sum (a multiple of kBatch)
 constexpr int kBatch = 8;      // independent loads in flight per lane in the line passes
 
-// x / 2, exactly: an exponent decrement for normal numbers, else a multiply.
+// x / 2 rounded to nearest even, on the IEEE fields with integer operations
+// only: an exponent decrement for normal numbers, a mantissa shift for the rest
+// (an FP64 multiply here would be if-converted into every element's path and
+// cost the FP64 pipe more than the element's own multiply-adds).  Inf and NaN
+// keep their exponent field and stay what they are.
 __device__ __forceinline__ double half_exact(double x) {
-    const long long b = __double_as_longlong(x);
-    if (((b >> 52) & 0x7ff) > 1) return __longlong_as_double(b - (1ll << 52));
-    return x * 0.5;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long ex = (b >> 52) & 0x7ff;
+    if (ex > 1 && ex < 0x7ff) return __longlong_as_double((long long)(b - (1ull << 52)));
+    if (ex == 0x7ff) return x;
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (ex << 52); // ex = 1: the implicit one
+    const unsigned long long h = (m >> 1) + (m & (m >> 1) & 1ull);     // halve, ties to even
+    return __longlong_as_double((long long)((b & 0x8000000000000000ull) | h));
 }
 
 // Scale exponent of a set whose largest |x| has IEEE bits mx: |x| < 2^e
@@ -146,28 +153,14 @@ struct FockScratch {
     double *S4;      // [q][p][r]   T4: sum over s
     double *S2;      // [r][p][s]   T2: sum over q
     double *S5;      // [p][r][s]   T5: sum over q
-    double *X3;      // [p][r][sc]  T3: per chunk of 32 s
-    double *X6;      // [q][ps][s]  T6: per quarter of p
+    double *X3;      // [p][r][s]   T3: sum over q
+    double *X6;      // [q][p][s]   T6: sum over r
     double *YJ;      // [i][j], i >= j
     double *XK;      // [i][j]
     const float *Dd; // split form: [row][k][S] digits of D
     const int *De;   //             [row] scale exponents of D's rows
     int nsc;         // chunks of 32 s
 };
-
-// Unit x of the line passes, the largest p first: (p, group of kWarps r).
-__device__ __forceinline__ void unit_pr(int x, int n, int &p, int &rg) {
-    int total = 0;
-    for (int pp = 0; pp < n; pp++) total += (pp + kWarps) / kWarps;
-    x = total - 1 - x;
-    int cum = 0;
-    for (p = 0; p < n; p++) {
-        const int c = (p + kWarps) / kWarps;
-        if (x < cum + c) break;
-        cum += c;
-    }
-    rg = x - cum;
-}
 
 // Digits of every row of D at the row's own scale: De[row] with |D[row][k]| < 2^e.
 template <int S>
@@ -193,24 +186,59 @@ __global__ void __launch_bounds__(128) k_fock_digits_d(const double *__restrict_
 
 constexpr int kShift(int S) { return -2 * split::kTopBits - split::kBits * (S - 1); }
 
-// T1 and T4.  Warp (p, r), lane q: sums over s <= r (s <= q when p == r) of
-// f g[p,q,r,s] {D[r,s], D[p,s]}, reading g[r,s,p,q] -- lanes along q.  The
-// loop runs over the warp's common range in batches of kBatch independent
-// loads (a lane outside its own range adds nothing), so that each warp keeps
-// kBatch reads in flight instead of one.
+// Flattened lanes.  For the rows pass, one r and the pairs (p, q) with p >= r,
+// q <= p, numbered p-major from 0: pair f has p with start(p) <= f < start(p + 1),
+// start(p) = (p (p + 1) - r (r + 1)) / 2.  For the columns pass, one p and the
+// pairs (r, s) with s <= r <= p: start(r) = r (r + 1) / 2.  Consecutive lanes take
+// consecutive pairs, so warps stay full however small p or r is.
+__device__ __forceinline__ int tri_row(long long K) { // largest x with x (x + 1) <= K
+    int x = (int)((sqrtf(4.0f * (float)K + 1.0f) - 1.0f) * 0.5f);
+    while ((long long)(x + 1) * (x + 2) <= K) x++;
+    while (x > 0 && (long long)x * (x + 1) > K) x--;
+    return x;
+}
+
+// CTA x of a pass whose units u = 0 .. n-1 have count(u) pairs: the unit and the
+// first pair of the CTA (kWarps * 32 pairs per CTA; the units with more pairs first).
+template <typename Count>
+__device__ __forceinline__ void unit_of_cta(int x, int n, Count count, int &u, int &first) {
+    for (int k = 0; k < n; k++) {
+        const int uu = n - 1 - k;
+        const int ctas = (count(uu) + kWarps * 32 - 1) / (kWarps * 32);
+        if (x < ctas) {
+            u = uu;
+            first = x * kWarps * 32;
+            return;
+        }
+        x -= ctas;
+    }
+    u = -1;
+    first = 0;
+}
+
+__device__ __forceinline__ int rows_pairs(int n, int r) { return (n * (n + 1) - r * (r + 1)) / 2; }
+__device__ __forceinline__ int cols_pairs(int p) { return (p + 1) * (p + 2) / 2; }
+
+// T1 and T4.  Unit r, lane (p, q): sums over s <= r (s <= q when p == r) of
+// f g[p,q,r,s] {D[r,s], D[p,s]}, reading g[r,s,p,q] -- consecutive lanes read
+// consecutive q.  The loop runs over the warp's common range in batches of
+// kBatch independent loads (a lane outside its own range adds nothing).
 template <int S>
 __global__ void __launch_bounds__(kWarps * 32) k_fock_rows(const double *__restrict__ g,
                                                            const double *__restrict__ D, int n, FockScratch sc) {
-    int p, rg;
-    unit_pr(blockIdx.x, n, p, rg);
-    const int r = rg * kWarps + (threadIdx.x >> 5);
-    const int q = blockIdx.y * 32 + (threadIdx.x & 31);
-    if (r > p || (int)blockIdx.y * 32 > p) return; // whole warps leave together
-    const bool on = q <= p;
+    int r, first;
+    unit_of_cta(blockIdx.x, n, [&](int u) { return rows_pairs(n, u); }, r, first);
+    if (r < 0) return;
+    const int f = first + threadIdx.x;
+    const bool on = f < rows_pairs(n, r);
+    int p = tri_row(2ll * (on ? f : 0) + (long long)r * (r + 1));
+    if (p < r) p = r;
+    if (p >= n) p = n - 1;
+    const int q = on ? f - (p * (p + 1) - r * (r + 1)) / 2 : 0;
     const bool diag = p == r;
     const int smax = diag ? q : r; // this lane's last s
     const size_t step = (size_t)n * n; // s -> s + 1 in g[r][s][p][q]
-    const double *gl = g + (((size_t)r * n) * n + p) * n + (on ? q : p);
+    const double *gl = g + (((size_t)r * n) * n + p) * n + q;
     const double *Dr = D + (size_t)r * n, *Dp = D + (size_t)p * n;
     auto scale = [&](double v, int s) {
         if (q == p) v = half_exact(v);
@@ -285,25 +313,26 @@ __global__ void __launch_bounds__(kWarps * 32) k_fock_rows(const double *__restr
     }
 }
 
-// T2, T5 and T3.  Warp (p, r), lane s <= r: sums over q <= p (q >= s when p == r)
-// of f g[p,q,r,s] {D[p,q], D[r,q], D[q,s]} -- lanes along s, batches of
-// kBatch loads as in the rows pass.  T3 adds up across the warp (one total per
-// chunk of 32 s).
+// T2, T5 and T3.  Unit p, lane (r, s): sums over q <= p (q >= s when p == r) of
+// f g[p,q,r,s] {D[p,q], D[q,r], D[q,s]} -- consecutive lanes read consecutive s;
+// batches of kBatch loads as in the rows pass.  Each lane's T3 sum over q is
+// added over s by the reduction.
 template <int S>
 __global__ void __launch_bounds__(kWarps * 32) k_fock_cols(const double *__restrict__ g,
                                                            const double *__restrict__ D, int n, FockScratch sc) {
-    int p, rg;
-    unit_pr(blockIdx.x, n, p, rg);
-    const int r = rg * kWarps + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
-    const int s = blockIdx.y * 32 + lane;
-    if (r > p || (int)blockIdx.y * 32 > r) return; // whole warps leave together
-    const bool on = s <= r;
+    int p, first;
+    unit_of_cta(blockIdx.x, n, [&](int u) { return cols_pairs(u); }, p, first);
+    if (p < 0) return;
+    const int f = first + threadIdx.x;
+    const bool on = f < cols_pairs(p);
+    int r = tri_row(2ll * (on ? f : 0));
+    if (r > p) r = p;
+    const int s = on ? f - r * (r + 1) / 2 : 0;
     const bool diag = p == r;
     const int qmin = diag ? s : 0; // this lane's first q
     const size_t step = (size_t)n * n; // q -> q + 1 in g[p][q][r][s]
-    const double *gl = g + (((size_t)p * n) * n + r) * n + (on ? s : r);
-    const double *Dp = D + (size_t)p * n, *Dr = D + (size_t)r * n;
+    const double *gl = g + (((size_t)p * n) * n + r) * n + s;
+    const double *Dp = D + (size_t)p * n;
     auto scale = [&](double v, int q) {
         if (q == p) v = half_exact(v);
         if (s == r) v = half_exact(v);
@@ -323,7 +352,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_fock_cols(const double *__restr
                 if (q <= p && q >= qmin && on) {
                     const double w = scale(v[u], q);
                     a2 = fma(w, __ldg(Dp + q), a2);
-                    a5 = fma(w, __ldg(Dr + q), a5);
+                    a5 = fma(w, __ldg(D + (size_t)q * n + r), a5);
                     a3 = fma(w, __ldg(D + (size_t)q * n + s), a3);
                 }
             }
@@ -377,56 +406,44 @@ __global__ void __launch_bounds__(kWarps * 32) k_fock_cols(const double *__restr
     if (on) {
         sc.S2[((size_t)r * n + p) * n + s] = v2;
         sc.S5[((size_t)p * n + r) * n + s] = v5;
+        sc.X3[((size_t)p * n + r) * n + s] = a3;
     }
-    for (int o = 16; o > 0; o >>= 1) a3 += __shfl_down_sync(0xffffffffu, a3, o);
-    if (lane == 0) sc.X3[((size_t)p * n + r) * sc.nsc + blockIdx.y] = a3;
 }
 
 // T6: XK[q,s] = sum over canonical (p, r) -- p >= q, s <= r <= p, without r = p
-// when q < s -- of f g[q,p,r,s] D[p,r].  CTA (q, 32 s, quarter ps of p): lane = s,
-// warps interleaved over p; the four warps' sums are added in warp order.
+// when q < s -- of f g[q,p,r,s] D[p,r].  Warp (q, 32 s, p), lane = s: the sum
+// over r for one p, so that every warp has at most n terms (the sums over p
+// would leave a few long warps running alone); the reduction adds over p.
 __global__ void __launch_bounds__(kWarps * 32) k_fock_exchange(const double *__restrict__ g,
                                                                const double *__restrict__ D, int n, int nsc,
                                                                double *__restrict__ X6) {
     const int q = blockIdx.x / nsc, s0 = (blockIdx.x - q * nsc) * 32;
-    const int ps = blockIdx.y;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int s = s0 + lane;
-    __shared__ double part[kWarps][32];
+    const int p = blockIdx.y * kWarps + (threadIdx.x >> 5);
+    const int s = s0 + (threadIdx.x & 31);
+    if (p >= n || p < q || p < s0) return; // whole warps leave together
+    const int sl = s < n ? s : n - 1;
+    const int rend = s >= n ? -1 : (q < s ? p - 1 : p); // this lane's canonical r in [s, rend]
+    const double *gl = g + (((size_t)q * n + p) * n) * n + sl;
+    const double *Dp = D + (size_t)p * n;
     double acc = 0.0;
-    {
-        // the warp walks r over [s0, p] in batches of kBatch loads; a lane adds only
-        // its canonical r in [s, rend]
-        const int sl = s < n ? s : n - 1;
-        for (int p = max(q, s0) + ps + kExPSplit * warp; p < n; p += kExPSplit * kWarps) {
-            const int rend = s >= n ? -1 : (q < s ? p - 1 : p);
-            const double *gl = g + (((size_t)q * n + p) * n) * n + sl;
-            const double *Dp = D + (size_t)p * n;
-            for (int r0 = s0; r0 <= p; r0 += kBatch) {
-                double v[kBatch];
+    // the warp walks r over [s0, p] in batches of kBatch loads
+    for (int r0 = s0; r0 <= p; r0 += kBatch) {
+        double v[kBatch];
 #pragma unroll
-                for (int u = 0; u < kBatch; u++) v[u] = r0 + u <= p ? __ldcs(gl + (size_t)(r0 + u) * n) : 0.0;
+        for (int u = 0; u < kBatch; u++) v[u] = r0 + u <= p ? __ldcs(gl + (size_t)(r0 + u) * n) : 0.0;
 #pragma unroll
-                for (int u = 0; u < kBatch; u++) {
-                    const int r = r0 + u;
-                    if (r >= s && r <= rend) {
-                        double w = v[u];
-                        if (p == q) w = half_exact(w);
-                        if (r == s) w = half_exact(w);
-                        if (p == r && q == s) w = half_exact(w);
-                        acc = fma(w, __ldg(Dp + r), acc);
-                    }
-                }
+        for (int u = 0; u < kBatch; u++) {
+            const int r = r0 + u;
+            if (r >= s && r <= rend) {
+                double w = v[u];
+                if (p == q) w = half_exact(w);
+                if (r == s) w = half_exact(w);
+                if (p == r && q == s) w = half_exact(w);
+                acc = fma(w, __ldg(Dp + r), acc);
             }
         }
     }
-    part[warp][lane] = acc;
-    __syncthreads();
-    if (warp == 0 && s < n) {
-        double t = part[0][lane];
-        for (int w = 1; w < kWarps; w++) t += part[w][lane];
-        X6[((size_t)q * kExPSplit + ps) * n + s] = t;
-    }
+    if (s < n) X6[((size_t)q * n + p) * n + s] = acc;
 }
 
 // Row i, columns j of one chunk of 32, of YJ (j <= i) and XK from the partials.
@@ -441,12 +458,12 @@ __global__ void __launch_bounds__(kRedWarps * 32) k_fock_reduce(int n, FockScrat
     if (j < n) {
         double xk = 0.0, yj = 0.0;
         if (warp == 0) {
-            for (int ps = 0; ps < kExPSplit; ps++) xk += sc.X6[((size_t)i * kExPSplit + ps) * n + j];
-            if (i >= j)
-                for (int c = 0; c * 32 <= j; c++) xk += sc.X3[((size_t)i * n + j) * sc.nsc + c];
+
         }
         for (int t = warp; t < n; t += kRedWarps) {
             if (t >= max(i, j)) xk += sc.S4[((size_t)i * n + t) * n + j]; // T4 of (p = t, r = j), q = i
+            if (t >= max(i, j & ~31)) xk += sc.X6[((size_t)i * n + t) * n + j]; // T6 of (q = i, p = t), s = j
+            if (i >= j && t <= j) xk += sc.X3[((size_t)i * n + j) * n + t];      // T3 of (p = i, r = j), s = t
             if (i >= j) {
                 if (t >= j && t <= i) xk += sc.S5[((size_t)i * n + t) * n + j]; // T5 of (p = i, r = t), s = j
                 if (t <= i) yj += sc.S1[((size_t)i * n + t) * n + j];           // T1 of (p = i, r = t), q = j
@@ -484,9 +501,11 @@ __global__ void __launch_bounds__(128) k_fock_combine(double *F, int n, FockScra
 
 template <int S>
 eg_status launch_lines(const double *g, const double *D, int n, const FockScratch &sc, cudaStream_t s) {
-    int units = 0;
-    for (int p = 0; p < n; p++) units += (p + kWarps) / kWarps;
-    const unsigned chunks = (unsigned)((n + 31) / 32);
+    unsigned rows_ctas = 0, cols_ctas = 0;
+    for (int u = 0; u < n; u++) {
+        rows_ctas += (unsigned)(((n * (n + 1) - u * (u + 1)) / 2 + kWarps * 32 - 1) / (kWarps * 32));
+        cols_ctas += (unsigned)(((u + 1) * (u + 2) / 2 + kWarps * 32 - 1) / (kWarps * 32));
+    }
     if constexpr (S > 0) {
         {
             LaunchScope ls_("k_fock_digits_d", s);
@@ -496,12 +515,12 @@ eg_status launch_lines(const double *g, const double *D, int n, const FockScratc
     }
     {
         LaunchScope ls_("k_fock_rows", s);
-        k_fock_rows<S><<<dim3((unsigned)units, chunks), kWarps * 32, 0, s>>>(g, D, n, sc);
+        k_fock_rows<S><<<rows_ctas, kWarps * 32, 0, s>>>(g, D, n, sc);
     }
     EG_CHECK_LAUNCH("k_fock_rows");
     {
         LaunchScope ls_("k_fock_cols", s);
-        k_fock_cols<S><<<dim3((unsigned)units, chunks), kWarps * 32, 0, s>>>(g, D, n, sc);
+        k_fock_cols<S><<<cols_ctas, kWarps * 32, 0, s>>>(g, D, n, sc);
     }
     EG_CHECK_LAUNCH("k_fock_cols");
     return EG_SUCCESS;
@@ -533,7 +552,7 @@ extern "C" eg_status eg_fock_jk_symmetric(double F_prefactor, double *F, double 
     const int nn = (int)n;
     const int nsc = (nn + 31) / 32;
     const size_t n3 = (size_t)nn * nn * nn, n2 = (size_t)nn * nn;
-    const size_t elems = 4 * n3 + n2 * nsc + n2 * kExPSplit + 2 * n2;
+    const size_t elems = 6 * n3 + 2 * n2;
     const size_t dd_bytes = S ? (n2 * S * sizeof(float) + (size_t)nn * sizeof(int) + 256) : 0;
     cudaStream_t s = (cudaStream_t)stream;
     void *ws = nullptr;
@@ -545,8 +564,8 @@ extern "C" eg_status eg_fock_jk_symmetric(double F_prefactor, double *F, double 
     sc.S2 = sc.S4 + n3;
     sc.S5 = sc.S2 + n3;
     sc.X3 = sc.S5 + n3;
-    sc.X6 = sc.X3 + n2 * nsc;
-    sc.YJ = sc.X6 + n2 * kExPSplit;
+    sc.X6 = sc.X3 + n3;
+    sc.YJ = sc.X6 + n3;
     sc.XK = sc.YJ + n2;
     sc.Dd = S ? (const float *)(sc.XK + n2) : nullptr;
     sc.De = S ? (const int *)(sc.Dd + n2 * S) : nullptr;
@@ -561,7 +580,8 @@ extern "C" eg_status eg_fock_jk_symmetric(double F_prefactor, double *F, double 
     if (st != EG_SUCCESS) return st;
     {
         LaunchScope ls_("k_fock_exchange", s);
-        k_fock_exchange<<<dim3((unsigned)(nn * nsc), kExPSplit), kWarps * 32, 0, s>>>(g, D, nn, nsc, sc.X6);
+        k_fock_exchange<<<dim3((unsigned)(nn * nsc), (unsigned)((nn + kWarps - 1) / kWarps)), kWarps * 32, 0, s>>>(
+            g, D, nn, nsc, sc.X6);
     }
     EG_CHECK_LAUNCH("k_fock_exchange");
     {

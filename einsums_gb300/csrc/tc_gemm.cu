@@ -45,6 +45,9 @@ constexpr int STAGE_BYTES = GROUP_KB * KB_BYTES;  // [A kb0][A kb1][B kb0][B kb1
 constexpr int THREADS = 320; // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int AUX_BYTES = 256;
+#ifndef EG_PREFETCH_C
+#define EG_PREFETCH_C 0
+#endif
 constexpr int kFinCols = 8;  // columns of the pending tile finished per chunk (C transposed through shared memory)
 // When C is contiguous along the rows (one thread per row): 4 columns per chunk;
 // 8 measured 10 % slower on the CCD Wabef contraction (more registers spilled).
@@ -642,6 +645,25 @@ __global__ void __launch_bounds__(THREADS, 1)
             rowOffW[lane] = rowOff;
             rowOkW[lane] = row_ok ? 1 : 0;
             __syncwarp();
+#if EG_PREFETCH_C
+            // The pending tile's C is read during the next tile's chunks: ask for its
+            // lines in L2 now, so that those reads wait on L2, not on DRAM.
+            if (finish && !direct && !plain_store) {
+                const bool fast = job.mg->n > 0 && job.mg->s[2][job.mg->n - 1] == 1;
+                if (fast) {
+                    // C runs along the rows: a 128-byte line holds 16 of this warp's rows
+                    if (row_ok && (lane & 15) == 0)
+                        for (int c = 0; c < kBN / 2; c++)
+                            if (colExp[c] != INT_MAX)
+                                asm volatile("prefetch.global.L2 [%0];" ::"l"(job.C + rowOff + colOff[c]));
+                } else if (row_ok) {
+                    // C runs along the columns: a line holds 16 of this row's columns
+                    for (int c = 0; c < kBN / 2; c += 16)
+                        if (colExp[c] != INT_MAX)
+                            asm volatile("prefetch.global.L2 [%0];" ::"l"(job.C + rowOff + colOff[c]));
+                }
+            }
+#endif
             if (direct) {
                 // the same conversion and stores as finalize_cols, the sums read from TMEM
                 const bool rows_fast = job.mg->n > 0 && job.mg->s[2][job.mg->n - 1] == 1;

@@ -101,6 +101,21 @@ eg_status eg_einsum(double C_prefactor, const int32_t *C_labels, const eg_tensor
                     const eg_options *opt, void *stream, int32_t *algorithm_choice);
 
 /*
+ * Complex128 einsum: C = C_prefactor * C + AB_prefactor * sum_links op(A) * op(B), where op
+ * conjugates A when conj_A != 0 and B when conj_B != 0.  C, A and B point to interleaved
+ * (real, imaginary) doubles; their extents and strides count complex elements.  C_prefactor and
+ * AB_prefactor are (real, imaginary) pairs.  Replaces einsum<ConjA, ConjB>(...) on
+ * std::complex<double> tensors (Backends/Dispatch.hpp:48,136, conjugation in the generic loops
+ * of Backends/BaseAlgebra.hpp:33-38).  Runs as the real contractions of the parts' strided views
+ * through eg_einsum (four when AB_prefactor is real, eight otherwise), with opt's precision; a
+ * complex C_prefactor is applied to C first.  *algorithm_choice: the choice for the pattern.
+ */
+eg_status eg_einsum_complex(const double *C_prefactor, const int32_t *C_labels, const eg_tensor *C,
+                            const double *AB_prefactor, const int32_t *A_labels, const eg_tensor *A,
+                            const int32_t *B_labels, const eg_tensor *B, int32_t conj_A, int32_t conj_B,
+                            const eg_options *opt, void *stream, int32_t *algorithm_choice);
+
+/*
  * Algorithm choice of a pattern without running it (no stride vetoes).
  * Replaces the dry-run dispatch detail::einsum<false, true, ...>
  * (Backends/Dispatch.hpp:1276-1279) and compile_plan's plan-type selection
@@ -266,9 +281,12 @@ eg_status eg_copy_to_host(void *dst, const void *src, size_t bytes, void *stream
 eg_status eg_stream_synchronize(void *stream);
 
 /* Measures FP64 throughput of this device (TFLOP/s) with a DFMA loop and an
- * mma.sync m8n8k4 f64 (DMMA) loop; synchronises the device.  The roofline
- * denominator of the plain FP64 form.  No reference counterpart. */
+ * mma.sync m8n8k4 f64 (DMMA) loop (best of three runs after a warm-up run);
+ * synchronises the device.  The roofline denominator of the plain FP64 form.
+ * eg_measure_fp64_peak_clock also gives the SM clock (MHz) the DFMA loop ran at,
+ * from its SM cycles over its duration.  No reference counterpart. */
 eg_status eg_measure_fp64_peak(double *dfma_tflops, double *dmma_tflops);
+eg_status eg_measure_fp64_peak_clock(double *dfma_tflops, double *dmma_tflops, double *probe_mhz);
 
 /* Kernel accounting.  eg_kernel_launches: kernels this library has launched in the
  * process.  With profiling on, every launch is bracketed by CUDA events on its own

@@ -85,3 +85,79 @@ def test_restated_symmetric_fock_matches_the_two_contractions(n, seed):
     K_ref = np.einsum("prqs,rs->pq", g, D)
     assert np.allclose(J, J_ref, rtol=1e-13, atol=1e-13 * np.abs(J_ref).max())
     assert np.allclose(K, K_ref, rtol=1e-13, atol=1e-13 * np.abs(K_ref).max())
+
+
+def _half_exact(x):
+    """half_exact of fock.cu: x / 2 with integer operations on the IEEE fields."""
+    import struct
+    b = struct.unpack("<Q", struct.pack("<d", x))[0]
+    ex = (b >> 52) & 0x7FF
+    if 1 < ex < 0x7FF:
+        b -= 1 << 52
+    elif ex != 0x7FF:
+        m = (b & 0xFFFFFFFFFFFFF) | (ex << 52)
+        h = (m >> 1) + (m & (m >> 1) & 1)
+        b = (b & 0x8000000000000000) | h
+    return struct.unpack("<d", struct.pack("<Q", b))[0]
+
+
+def test_half_exact_matches_the_rounded_half():
+    import struct
+    rng = np.random.default_rng(7)
+    bits = rng.integers(0, 2 ** 63, size=20000, dtype=np.uint64) * 2 + rng.integers(0, 2, size=20000, dtype=np.uint64)
+    bits[::3] &= np.uint64(0x801FFFFFFFFFFFFF)  # exponents near zero: subnormal results and their edge
+    xs = [struct.unpack("<d", struct.pack("<Q", int(b)))[0] for b in bits]
+    xs += [0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, 2.225073858507201e-308, 1.0, float("inf")]
+    for x in xs:
+        if np.isnan(x):
+            continue
+        assert struct.pack("<d", _half_exact(x)) == struct.pack("<d", x * 0.5), x
+
+
+def _tri_row(K):
+    x = int((np.sqrt(np.float32(4.0 * K + 1.0)) - 1.0) * 0.5)
+    while (x + 1) * (x + 2) <= K:
+        x += 1
+    while x > 0 and x * (x + 1) > K:
+        x -= 1
+    return x
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 33, 70])
+def test_flattened_lanes_cover_every_pair_once(n):
+    """The lane mapping of fock.cu's rows and columns passes: CTAs of 128 pairs,
+    units with more pairs first; every (p, q) of a rows unit r and every (r, s) of a
+    columns unit p is taken by exactly one lane."""
+    per_cta = 128
+    rows_pairs = lambda r: (n * (n + 1) - r * (r + 1)) // 2
+    cols_pairs = lambda p: (p + 1) * (p + 2) // 2
+    for count, kind in ((rows_pairs, "rows"), (cols_pairs, "cols")):
+        seen = set()
+        ctas = sum((count(u) + per_cta - 1) // per_cta for u in range(n))
+        for x in range(ctas):
+            k, xx = 0, x
+            for k in range(n):
+                u = n - 1 - k
+                c = (count(u) + per_cta - 1) // per_cta
+                if xx < c:
+                    break
+                xx -= c
+            first = xx * per_cta
+            for t in range(per_cta):
+                f = first + t
+                if f >= count(u):
+                    continue
+                if kind == "rows":
+                    r = u
+                    p = min(max(_tri_row(2 * f + r * (r + 1)), r), n - 1)
+                    q = f - (p * (p + 1) - r * (r + 1)) // 2
+                    assert r <= p < n and 0 <= q <= p
+                    seen.add((r, p, q))
+                else:
+                    p = u
+                    r = min(_tri_row(2 * f), p)
+                    s = f - r * (r + 1) // 2
+                    assert 0 <= s <= r <= p
+                    seen.add((p, r, s))
+        want = (sum(rows_pairs(r) for r in range(n)) if kind == "rows" else sum(cols_pairs(p) for p in range(n)))
+        assert len(seen) == want
