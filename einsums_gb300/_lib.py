@@ -108,6 +108,7 @@ PROTOTYPES = {
     "eg_stream_status": (ctypes.c_int, [ctypes.c_void_p, _P(ctypes.c_int32)]),
     "eg_measure_fp64_peak": (ctypes.c_int, [_P(ctypes.c_double), _P(ctypes.c_double)]),
     "eg_measure_fp64_peak_clock": (ctypes.c_int, [_P(ctypes.c_double), _P(ctypes.c_double), _P(ctypes.c_double)]),
+    "eg_tc_pair_clusters": (ctypes.c_int, [_P(ctypes.c_int32)]),
     "eg_kernel_launches": (ctypes.c_int, [_P(ctypes.c_uint64)]),
     "eg_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_void_p]),
     "eg_profile_enable": (ctypes.c_int, [ctypes.c_int32]),

@@ -35,6 +35,8 @@ eg_status lower_for_group(double cp, const int32_t *Cl, const eg_tensor *C, doub
                           const eg_tensor *A, const int32_t *Bl, const eg_tensor *B, const eg_options &opt,
                           Contraction &out, int32_t *alg_out, bool &gemm_shaped);
 eg_status encode_planes_public(CUtensorMap *map, void *base, int64_t Kp, int64_t rows, int64_t planes);
+eg_status encode_planes_extent(CUtensorMap *map, void *base, int64_t K, int64_t rows, int64_t planes, int64_t Kp,
+                               int64_t Rp);
 void set_capture_mode(bool on);
 void count_launches(uint64_t n);
 } // namespace eg
@@ -631,6 +633,22 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     CUtensorMap tmA, tmB;
     if ((st = encode_planes_public(&tmA, planesA, Kmaxp, Rmax, zA)) != EG_SUCCESS) return st;
     if ((st = encode_planes_public(&tmB, planesB, Kmaxp, Rmax, zB)) != EG_SUCCESS) return st;
+    // per-item maps: each item's planes with its own M (N) and K as the extents
+    std::vector<CUtensorMap> maps(2 * items.size());
+    for (size_t i = 0; i < items.size(); i++) {
+        const TcItem &it = items[i];
+        const Contraction &c = cs[i];
+        const int64_t planes = c.batch.total * S, K = c.k.total;
+        const size_t plane = (size_t)Rmax * Kmaxp;
+        if ((st = encode_planes_extent(&maps[2 * i], (__nv_bfloat16 *)planesA + (size_t)it.zA * plane, K, it.M, planes,
+                                       Kmaxp, Rmax)) != EG_SUCCESS)
+            return st;
+        if ((st = encode_planes_extent(&maps[2 * i + 1], (__nv_bfloat16 *)planesB + (size_t)it.zB * plane, K, it.N,
+                                       planes, Kmaxp, Rmax)) != EG_SUCCESS)
+            return st;
+    }
+    void *d_maps = nullptr;
+    if ((st = dev_copy(plan, maps.data(), maps.size() * sizeof(CUtensorMap), &d_maps)) != EG_SUCCESS) return st;
     int *status = nullptr;
     if ((st = status_word(s, &status)) != EG_SUCCESS) return st;
 
@@ -655,6 +673,8 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     p.timeout_ns = 2000ull * 1000 * 1000;
     p.ksplit = 1; // no K slicing in grouped launches
     p.kslice = 0;
+    static const bool shared_maps = std::getenv("EINSUMS_GB300_GROUPED_SHARED_MAPS") != nullptr;
+    p.item_maps = shared_maps ? nullptr : (const CUtensorMap *)d_maps;
     p.rbuf = (long long *)rbuf;
     static const bool prof_on = std::getenv("EINSUMS_GB300_TC_PROFILE") != nullptr;
     if (prof_on) {

@@ -261,13 +261,13 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     return fn;
 }
 
-// 3-D map over [planes][rows][Kp] BF16, box 64 (k) x 128 rows x 1, 128-byte swizzle.
-eg_status encode_planes(CUtensorMap *map, void *base, int64_t Kp, int64_t rows, int64_t planes) {
+// 3-D map over [planes][rows][Kp] BF16, box 64 (k) x box_rows rows x 1, 128-byte swizzle.
+eg_status encode_planes(CUtensorMap *map, void *base, int64_t Kp, int64_t rows, int64_t planes, int box_rows = kBM) {
     auto fn = encode_fn();
     if (!fn) return fail(EG_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
     cuuint64_t dims[3] = {(cuuint64_t)Kp, (cuuint64_t)rows, (cuuint64_t)planes};
     cuuint64_t strides[2] = {(cuuint64_t)(Kp * 2), (cuuint64_t)(Kp * 2 * rows)};
-    cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)kBM, 1};
+    cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -364,6 +364,24 @@ eg_status encode_planes_public(CUtensorMap *map, void *base, int64_t Kp, int64_t
     return split::encode_planes(map, base, Kp, rows, planes);
 }
 
+// A map over `planes` planes of `rows` x `K` BF16 digits laid out with row
+// stride Kp and plane stride Rp * Kp elements (the extents may be below the
+// padded layout: TMA then fills the rest of a box with zeros).
+eg_status encode_planes_extent(CUtensorMap *map, void *base, int64_t K, int64_t rows, int64_t planes, int64_t Kp,
+                               int64_t Rp) {
+    auto fn = split::encode_fn();
+    if (!fn) return fail(EG_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)planes};
+    cuuint64_t strides[2] = {(cuuint64_t)(Kp * 2), (cuuint64_t)(Kp * 2 * Rp)};
+    cuuint32_t box[3] = {(cuuint32_t)split::kBK, (cuuint32_t)split::kBM, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(EG_ERROR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return EG_SUCCESS;
+}
+
 eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s, eg_split_report *rep) {
     using namespace split;
     const int S = slices ? slices : 5;
@@ -388,6 +406,9 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     // K slices in parallel when the output has fewer tiles than half the SMs
     const int64_t tiles = nb * (Mp / kBM) * (Np / kBN);
     const bool kslicing = tiles < num_sms() / 2;
+    // CTA pairs (256x128 tiles) whenever the output has two or more row tiles
+    const int clusters = Mp / kBM >= 2 ? tc_pair_clusters() : 0;
+    const bool pair = clusters > 0;
     const size_t offRacc = round_up((int64_t)(offTab + tabBytes), 256);
     const size_t raccBytes = kslicing ? (size_t)tiles * kBM * kBN * 8 : 0;
     const size_t offRcnt = offRacc + raccBytes;
@@ -413,9 +434,10 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
 
     CUtensorMap tmA, tmB;
     if ((st = encode_planes(&tmA, planesA, Kp, Mp, nb * S)) != EG_SUCCESS) return st;
-    if ((st = encode_planes(&tmB, planesB, Kp, Np, nb * S)) != EG_SUCCESS) return st;
+    if ((st = encode_planes(&tmB, planesB, Kp, Np, nb * S, pair ? kBN / 2 : kBN)) != EG_SUCCESS) return st;
 
     TcGemmParams p{};
+    p.pair = pair ? 1 : 0;
     p.S = S;
     p.mtiles = (int)(Mp / kBM);
     p.ntiles = (int)(Np / kBN);
@@ -459,11 +481,14 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
         p.ksplit = 1;
         p.kslice = p.nkb;
         if (kslicing && p.nkb >= 32) {
+            // schedule units: tiles over SMs, or pair tiles over CTA pairs
+            const int64_t units = pair ? nb * ((Mp / kBM + 1) / 2) * (Np / kBN) : tiles;
+            const int64_t workers = pair ? clusters : num_sms();
             int64_t best = -1;
             for (int ks = 1; ks <= p.nkb / 16; ks++) {
                 const int64_t slice = round_up((p.nkb + ks - 1) / ks, kKStep / kBK);
                 const int64_t n = (p.nkb + slice - 1) / slice; // slices actually used
-                const int64_t rounds = (tiles * n + num_sms() - 1) / num_sms();
+                const int64_t rounds = (units * n + workers - 1) / workers;
                 const int64_t cost = rounds * (slice + 4);
                 if (best < 0 || cost < best) {
                     best = cost;

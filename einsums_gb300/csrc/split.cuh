@@ -64,6 +64,13 @@ struct TcGemmParams {
     int ksplit, kslice;
     long long *racc;
     int *rcnt;
+    // Launch as CTA pairs (cta_group::2, 256x128 tiles; B's tensor map has
+    // 64-row boxes): single contractions only.
+    int pair;
+    // Grouped launches: two tensor maps per item (A, B) over the item's own digit
+    // planes with its own row and K extents, so that TMA fills the tile's rows
+    // past M (N) and K blocks past K with zeros instead of reading the padding.
+    const CUtensorMap *item_maps;
 };
 
 // One item of a grouped launch: an independent contraction whose digit planes
@@ -189,6 +196,9 @@ __device__ __forceinline__ void digits_bf16x2(double x0, double x1, int e, uint3
 
 // Sets the kernels' shared-memory attribute once (call outside stream capture).
 eg_status ensure_tc_attributes();
+// Clusters of two k_tc_split_gemm CTAs that fit on the GPU at once, when CTA
+// pairs are requested with EINSUMS_GB300_TC_PAIRS=1 (else 0: single-CTA tiles).
+int tc_pair_clusters();
 eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p, cudaStream_t s);
 // Grouped form: `ntiles_total` work entries, per-tile parameters from `items`.
 eg_status launch_tc_gemm_grouped(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p,

@@ -36,18 +36,11 @@ namespace eg::split {
 
 namespace {
 
-constexpr int STAGES = 3;                  // ring slots
 constexpr int GROUP_KB = 2;                // K blocks per slot
 constexpr int A_BYTES = kBM * kBK * 2;     // one K block of A (16 KB)
-constexpr int B_BYTES = kBN * kBK * 2;     // one K block of B (16 KB)
-constexpr int KB_BYTES = A_BYTES + B_BYTES;
-constexpr int STAGE_BYTES = GROUP_KB * KB_BYTES;  // [A kb0][A kb1][B kb0][B kb1]
 constexpr int THREADS = 320; // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int AUX_BYTES = 256;
-#ifndef EG_PREFETCH_C
-#define EG_PREFETCH_C 0
-#endif
 constexpr int kFinCols = 8;  // columns of the pending tile finished per chunk (C transposed through shared memory)
 // When C is contiguous along the rows (one thread per row): 4 columns per chunk;
 // 8 measured 10 % slower on the CCD Wabef contraction (more registers spilled).
@@ -57,7 +50,20 @@ constexpr int FIN_T = 33;    // padded row count of a warp's transposition buffe
 // per epilogue warp: 64 column offsets and exponents, the transposition buffer
 // of one batch, and its 32 rows' output offsets and validity
 constexpr int EPI_WARP_BYTES = (kBN / 2) * (8 + 4) + kFinCols * FIN_T * 8 + 32 * (8 + 4);
-constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + AUX_BYTES + 8 * EPI_WARP_BYTES + 64;
+
+// Ring geometry.  CL = 1: one CTA per 128x128 output tile; a slot holds
+// [A kb0][A kb1][B kb0][B kb1] (64 KB), three slots.  CL = 2: a CTA pair
+// computes a 256x128 tile with cta_group::2 MMAs (M = 256); each CTA holds its
+// own 128 rows of A and half of B (64 rows), so a slot is 48 KB and four fit.
+template <int CL>
+struct Ring {
+    static constexpr int STAGES = CL == 2 ? 4 : 3;
+    static constexpr int B_ROWS = kBN / CL;
+    static constexpr int B_BYTES = B_ROWS * kBK * 2; // one K block of this CTA's part of B
+    static constexpr int STAGE_BYTES = GROUP_KB * (A_BYTES + B_BYTES);
+    static constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + AUX_BYTES + 8 * EPI_WARP_BYTES + 64;
+};
+static_assert(Ring<1>::SMEM_BYTES <= 232448 && Ring<2>::SMEM_BYTES <= 232448, "shared memory per CTA");
 constexpr int GROUP_M = 16; // tile rasterisation: groups of 16 row tiles share B tiles in L2
 constexpr unsigned long long DRAIN_NS = 200ull * 1000 * 1000;
 
@@ -69,14 +75,18 @@ __device__ __forceinline__ void prof_add(const TcGemmParams &p, int slot, long l
     if (p.prof) atomicAdd(p.prof + blockIdx.x * kProfSlots + slot, (unsigned long long)cycles);
 }
 
+// Output tile t of the schedule in units of CL row tiles (a CTA pair takes two
+// vertically adjacent 128-row tiles); mt counts those units.
+template <int CL>
 __device__ __forceinline__ void tile_coords(const TcGemmParams &p, int t, int &b, int &mt, int &nt) {
-    const int per_batch = p.mtiles * p.ntiles;
+    const int mtiles = (p.mtiles + CL - 1) / CL, gm = GROUP_M / CL;
+    const int per_batch = mtiles * p.ntiles;
     b = t / per_batch;
     t -= b * per_batch;
-    const int per_group = GROUP_M * p.ntiles;
+    const int per_group = gm * p.ntiles;
     const int g = t / per_group;
-    const int first_m = g * GROUP_M;
-    const int gsize = min(p.mtiles - first_m, GROUP_M);
+    const int first_m = g * gm;
+    const int gsize = min(mtiles - first_m, gm);
     const int r = t - g * per_group;
     mt = first_m + r % gsize;
     nt = r / gsize;
@@ -89,27 +99,31 @@ struct TileJob {
     int zA, zB;  // digit plane of slice 0 for A / B
     int kbeg;    // first K block (of this pass) of the K slice
     int nkb;     // K blocks
-    int tid;     // linear output tile index (single-contraction form)
+    int tid;     // linear output tile index (single-contraction form); -1: rows past the
+                 // last tile (the odd half of a CTA pair's tile), nothing to store
     int64_t M, N;
     const ModeGroup *mg, *ng;
     const int *eA, *eB; // exponents of rows / columns of this (item, batch)
     double *C;          // output base of this (item, batch)
+    const CUtensorMap *mapA, *mapB; // per-item maps (grouped launches), else null
 };
 
-// Tile t of the schedule.
-template <bool GROUPED>
-__device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *items, const int4 *work, int t) {
+// Tile t of the schedule, as seen by CTA `rank` of its pair (0 when CL = 1).
+template <bool GROUPED, int CL>
+__device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *items, const int4 *work, int t,
+                                           int rank) {
     TileJob j;
     if (!GROUPED) {
-        int b;
+        int b, mu;
         const int ks = t % p.ksplit;
         t /= p.ksplit;
-        tile_coords(p, t, b, j.mt, j.nt);
+        tile_coords<CL>(p, t, b, mu, j.nt);
+        j.mt = mu * CL + rank;
         j.zA = b * p.S;
         j.zB = b * p.S;
         j.kbeg = ks * p.kslice;
         j.nkb = min(p.kslice, p.nkb - j.kbeg);
-        j.tid = (b * p.mtiles + j.mt) * p.ntiles + j.nt;
+        j.tid = j.mt < p.mtiles ? (b * p.mtiles + j.mt) * p.ntiles + j.nt : -1;
         j.M = p.M;
         j.N = p.N;
         j.mg = &p.mg;
@@ -119,14 +133,22 @@ __device__ __forceinline__ TileJob resolve(const TcGemmParams &p, const TcItem *
         int64_t oa, ob, oc;
         group_offsets(p.bg, b, oa, ob, oc);
         j.C = p.C + oc;
+        j.mapA = j.mapB = nullptr;
     } else {
         const int4 w = work[t];
         const TcItem &it = items[w.x];
         const int b = w.y;
         j.mt = w.z;
         j.nt = w.w;
-        j.zA = it.zA + b * p.S;
-        j.zB = it.zB + b * p.S;
+        if (p.item_maps) { // planes numbered within the item
+            j.mapA = p.item_maps + 2 * w.x;
+            j.mapB = j.mapA + 1;
+            j.zA = j.zB = b * p.S;
+        } else {
+            j.mapA = j.mapB = nullptr;
+            j.zA = it.zA + b * p.S;
+            j.zB = it.zB + b * p.S;
+        }
         j.kbeg = 0;
         j.nkb = it.nkb;
         j.tid = 0;
@@ -151,70 +173,78 @@ __device__ __forceinline__ int entry_nkb(const TcGemmParams &p, const TcItem *it
     return min(p.kslice, p.nkb - kbeg);
 }
 
-// Issues the 4 * NB MMAs of one group (K blocks at A/B descriptors a0, b0;
-// a second block sits A_BYTES / B_BYTES further on) and, in the same
-// instruction sequence, tests whether phase `parity` of the barrier at
+// The eight MMAs of one group (two K blocks at A/B descriptors a0, b0; the
+// second block sits A_BYTES / the slot's B block size further on) and, in the
+// same instruction sequence, a test of whether phase `parity` of the barrier at
 // `next_bar` has completed.  The test's result is read after the MMAs are
 // issued, so its latency overlaps their execution.
-template <int NB>
+#define EG_MMA_GROUP_ASM(CG)                                                                                           \
+    "{\n .reg .pred p, q;\n .reg .b64 a, b;\n setp.ne.b32 q, %4, 0;\n"                                              \
+    " mbarrier.test_wait.parity.shared::cta.b64 p, [%5], %6;\n"                                                        \
+    " tcgen05.mma.cta_group::" CG ".kind::f16 [%1], %2, %3, %7, q;\n"                                                  \
+    " tcgen05.mma.cta_group::" CG ".kind::f16 [%1], %8, %9, %7, 1;\n"                                                  \
+    " tcgen05.mma.cta_group::" CG ".kind::f16 [%1], %10, %11, %7, 1;\n"                                                \
+    " tcgen05.mma.cta_group::" CG ".kind::f16 [%1], %12, %13, %7, 1;\n"                                                \
+    " add.s64 a, %2, %14;\n add.s64 b, %3, %15;\n"                                                                     \
+    " tcgen05.mma.cta_group::" CG ".kind::f16 [%1], a, b, %7, 1;\n"                                                    \
+    " add.s64 a, %8, %14;\n add.s64 b, %9, %15;\n"                                                                     \
+    " tcgen05.mma.cta_group::" CG ".kind::f16 [%1], a, b, %7, 1;\n"                                                    \
+    " add.s64 a, %10, %14;\n add.s64 b, %11, %15;\n"                                                                   \
+    " tcgen05.mma.cta_group::" CG ".kind::f16 [%1], a, b, %7, 1;\n"                                                    \
+    " add.s64 a, %12, %14;\n add.s64 b, %13, %15;\n"                                                                   \
+    " tcgen05.mma.cta_group::" CG ".kind::f16 [%1], a, b, %7, 1;\n"                                                    \
+    " selp.u32 %0, 1, 0, p;\n}\n"
+
+template <int CL>
 __device__ __forceinline__ bool mma_group(uint32_t d, uint64_t a0, uint64_t b0, uint32_t idesc, uint32_t accumulate,
                                           uint32_t next_bar, uint32_t parity) {
-    static_assert(NB == 1 || NB == 2, "one or two K blocks per group");
-    constexpr uint64_t kStep = 32 >> 4;            // 16 BF16 along K
-    constexpr uint64_t aBlk = A_BYTES >> 4, bBlk = B_BYTES >> 4;
+    static_assert(GROUP_KB == 2, "two K blocks per group");
+    constexpr uint64_t kStep = 32 >> 4; // 16 BF16 along K
+    constexpr uint64_t aBlk = A_BYTES >> 4, bBlk = Ring<CL>::B_BYTES >> 4;
     uint32_t ok;
-    if (NB == 1) {
-        asm volatile(
-            "{\n .reg .pred p, q;\n setp.ne.b32 q, %4, 0;\n"
-            " mbarrier.test_wait.parity.shared::cta.b64 p, [%5], %6;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], %2, %3, %7, q;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], %8, %9, %7, 1;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], %10, %11, %7, 1;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], %12, %13, %7, 1;\n"
-            " selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(d), "l"(a0), "l"(b0), "r"(accumulate), "r"(next_bar), "r"(parity), "r"(idesc),
-              "l"(a0 + kStep), "l"(b0 + kStep), "l"(a0 + 2 * kStep), "l"(b0 + 2 * kStep), "l"(a0 + 3 * kStep),
-              "l"(b0 + 3 * kStep)
-            : "memory");
-    } else {
-        asm volatile(
-            "{\n .reg .pred p, q;\n .reg .b64 a, b;\n setp.ne.b32 q, %4, 0;\n"
-            " mbarrier.test_wait.parity.shared::cta.b64 p, [%5], %6;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], %2, %3, %7, q;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], %8, %9, %7, 1;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], %10, %11, %7, 1;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], %12, %13, %7, 1;\n"
-            " add.s64 a, %2, %14;\n add.s64 b, %3, %15;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], a, b, %7, 1;\n"
-            " add.s64 a, %8, %14;\n add.s64 b, %9, %15;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], a, b, %7, 1;\n"
-            " add.s64 a, %10, %14;\n add.s64 b, %11, %15;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], a, b, %7, 1;\n"
-            " add.s64 a, %12, %14;\n add.s64 b, %13, %15;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%1], a, b, %7, 1;\n"
-            " selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(ok)
-            : "r"(d), "l"(a0), "l"(b0), "r"(accumulate), "r"(next_bar), "r"(parity), "r"(idesc),
-              "l"(a0 + kStep), "l"(b0 + kStep), "l"(a0 + 2 * kStep), "l"(b0 + 2 * kStep), "l"(a0 + 3 * kStep),
-              "l"(b0 + 3 * kStep), "l"(aBlk), "l"(bBlk)
-            : "memory");
-    }
+#define EG_MMA_GROUP_OPERANDS                                                                                          \
+    : "=r"(ok)                                                                                                         \
+    : "r"(d), "l"(a0), "l"(b0), "r"(accumulate), "r"(next_bar), "r"(parity), "r"(idesc), "l"(a0 + kStep),             \
+      "l"(b0 + kStep), "l"(a0 + 2 * kStep), "l"(b0 + 2 * kStep), "l"(a0 + 3 * kStep), "l"(b0 + 3 * kStep), "l"(aBlk), \
+      "l"(bBlk)                                                                                                        \
+    : "memory"
+    if constexpr (CL == 1)
+        asm volatile(EG_MMA_GROUP_ASM("1") EG_MMA_GROUP_OPERANDS);
+    else
+        asm volatile(EG_MMA_GROUP_ASM("2") EG_MMA_GROUP_OPERANDS);
+#undef EG_MMA_GROUP_OPERANDS
     return ok != 0;
 }
+#undef EG_MMA_GROUP_ASM
 
-__device__ __forceinline__ void raise_abort(const TcGemmParams &p, volatile int *abort_flag, int code) {
+// Records `code` and stops this CTA's roles; in a CTA pair also the peer's
+// (peer_flag: shared::cluster address of its abort flag, 0 without a peer).
+__device__ __forceinline__ void raise_abort(const TcGemmParams &p, volatile int *abort_flag, int code,
+                                            uint32_t peer_flag = 0) {
     atomicCAS(p.status, 0, code);
     *abort_flag = 1;
+    if (peer_flag) ptx::st_cluster_u32(peer_flag, 1u);
 }
 
 // 10 warps: two of the four SM sub-partitions hold three warps, so the
 // 16K-register file of a sub-partition caps a thread at 168 registers.
-template <bool GROUPED>
+//
+// CL = 2 (launched as clusters of two CTAs): the pair computes 256x128 tiles.
+// Both CTAs run a TMA producer that loads its own 128 rows of A and its half of
+// B into its own ring, completing on the even CTA's "full" barrier (which
+// expects both CTAs' bytes); the even CTA's MMA issuer alone issues
+// cta_group::2 MMAs (M = 256) that read both CTAs' shared memory and write
+// each CTA's 128 rows into that CTA's tensor memory, and commits to the
+// "empty" and "accumulator full" barriers of both CTAs; both CTAs' epilogue
+// warps release an accumulator on the even CTA's barrier (16 arrivals).
+template <bool GROUPED, int CL>
 __global__ void __launch_bounds__(THREADS, 1)
     k_tc_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                     const __grid_constant__ TcGemmParams p, const TcItem *items, const int4 *work,
                     int ntiles_total) {
+    static_assert(CL == 1 || (CL == 2 && !GROUPED), "CTA pairs serve single contractions");
+    using R = Ring<CL>;
+    constexpr int STAGES = R::STAGES, STAGE_BYTES = R::STAGE_BYTES;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t *full = (uint64_t *)(smem + STAGES * STAGE_BYTES);
@@ -233,6 +263,11 @@ __global__ void __launch_bounds__(THREADS, 1)
     int *rowOkAll = (int *)(rowOffAll + 8 * 32);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rank = CL == 2 ? (int)ptx::cluster_ctarank() : 0;
+    // shared::cluster addresses: the even CTA's barriers, and the peer's abort flag
+    const uint32_t full_lead = CL == 2 ? ptx::mapa(ptx::smem_u32(full), 0) : 0;
+    const uint32_t acce_lead = CL == 2 ? ptx::mapa(ptx::smem_u32(acce), 0) : 0;
+    const uint32_t peer_flag = CL == 2 ? ptx::mapa(ptx::smem_u32((const void *)abort_flag), rank ^ 1) : 0;
     const long long t_start = p.prof ? clock64() : 0;
     if (threadIdx.x == 0) {
         for (int i = 0; i < STAGES; i++) {
@@ -241,23 +276,26 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         for (int i = 0; i < 2; i++) {
             ptx::mbar_init(&accf[i], 1);
-            ptx::mbar_init(&acce[i], 8);
+            ptx::mbar_init(&acce[i], 8 * CL);
         }
         ptx::mbar_init(done, 1);
         *abort_flag = 0;
         ptx::fence_mbar_init();
     }
     if (warp == 1) {
-        ptx::tmem_alloc(tmem_slot, TMEM_COLS);
-        ptx::tmem_relinquish();
+        ptx::tmem_alloc<CL>(tmem_slot, TMEM_COLS);
+        ptx::tmem_relinquish<CL>();
     }
     ptx::tc_fence_before();
     __syncthreads();
+    if (CL == 2) ptx::cluster_sync(); // the peer's barriers are initialised before any remote arrival
     ptx::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int cta0 = blockIdx.x, ctas = gridDim.x; // schedule index and stride of this CTA
+    // schedule index and stride of this CTA (of its pair when CL = 2)
+    const int cta0 = blockIdx.x / CL, ctas = gridDim.x / CL;
 
-    const int total_tiles = GROUPED ? ntiles_total : p.nbatch * p.mtiles * p.ntiles * p.ksplit;
+    const int total_tiles =
+        GROUPED ? ntiles_total : p.nbatch * ((p.mtiles + CL - 1) / CL) * p.ntiles * p.ksplit;
     const int S = p.S;
 
     if (warp == 0) {
@@ -267,10 +305,25 @@ __global__ void __launch_bounds__(THREADS, 1)
             ptx::tma_prefetch_desc(&tmB);
             int stage = 0;
             uint32_t phase = 0;
-            int issued = 0; // slots that have received a group (they fill in order 0, 1, 2)
+            int issued = 0; // slots that have received a group (they fill in order 0, 1, 2, ...)
             bool ok = true;
             for (int tile = cta0; tile < total_tiles && ok; tile += ctas) {
-                const TileJob job = resolve<GROUPED>(p, items, work, tile);
+                const TileJob job = resolve<GROUPED, CL>(p, items, work, tile, rank);
+                const int arow = job.mt * kBM, brow = job.nt * kBN + rank * R::B_ROWS;
+                const void *mA = &tmA, *mB = &tmB;
+                if (GROUPED && job.mapA) {
+                    mA = job.mapA;
+                    mB = job.mapB;
+                    if (tile + ctas < total_tiles) { // the next tile's maps, while this one runs
+                        const CUtensorMap *nm = p.item_maps + 2 * work[tile + ctas].x;
+                        ptx::tma_prefetch_desc(nm);
+                        ptx::tma_prefetch_desc(nm + 1);
+                    }
+                    if (tile == cta0) {
+                        ptx::tma_prefetch_desc(mA);
+                        ptx::tma_prefetch_desc(mB);
+                    }
+                }
                 for (int d = 0; d < S && ok; d++) {
                     for (int s = 0; s <= d && ok; s++) {
                         const int t = d - s;
@@ -279,18 +332,24 @@ __global__ void __launch_bounds__(THREADS, 1)
                             const bool got = ptx::mbar_wait(&empty[stage], phase ^ 1, p.timeout_ns, abort_flag);
                             if (p.prof) prof_add(p, kProfProducerWaitEmpty, clock64() - t0);
                             if (!got) {
-                                raise_abort(p, abort_flag, 1);
+                                raise_abort(p, abort_flag, 1, peer_flag);
                                 ok = false;
                                 break;
                             }
-                            ptx::mbar_arrive_expect_tx(&full[stage], (uint32_t)STAGE_BYTES);
+                            if (rank == 0) ptx::mbar_arrive_expect_tx(&full[stage], (uint32_t)(CL * STAGE_BYTES));
                             uint8_t *sa = smem + stage * STAGE_BYTES;
 #pragma unroll
                             for (int h = 0; h < GROUP_KB; h++) {
                                 const int kc = (p.kb0 + job.kbeg + kb + h) * kBK;
-                                ptx::tma_load_3d(sa + h * A_BYTES, &tmA, &full[stage], kc, job.mt * kBM, job.zA + s);
-                                uint8_t *sb = sa + GROUP_KB * A_BYTES + h * B_BYTES;
-                                ptx::tma_load_3d(sb, &tmB, &full[stage], kc, job.nt * kBN, job.zB + t);
+                                uint8_t *sb = sa + GROUP_KB * A_BYTES + h * R::B_BYTES;
+                                if (CL == 1) {
+                                    ptx::tma_load_3d(sa + h * A_BYTES, mA, &full[stage], kc, arow, job.zA + s);
+                                    ptx::tma_load_3d(sb, mB, &full[stage], kc, brow, job.zB + t);
+                                } else {
+                                    const uint32_t fb = full_lead + (uint32_t)(stage * 8);
+                                    ptx::tma_load_3d_pair(sa + h * A_BYTES, &tmA, fb, kc, arow, job.zA + s);
+                                    ptx::tma_load_3d_pair(sb, &tmB, fb, kc, brow, job.zB + t);
+                                }
                             }
                             if (issued < STAGES) issued++;
                             if (++stage == STAGES) {
@@ -302,23 +361,36 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
             }
             // Slot i last received a group in the current round of the ring if
-            // i < stage, else in the previous one.
-            for (int i = 0; i < issued; i++)
-                if (!ptx::mbar_wait(&full[i], i < stage ? phase : phase ^ 1, DRAIN_NS, nullptr))
-                    raise_abort(p, abort_flag, 4);
+            // i < stage, else in the previous one.  In a pair the even CTA's
+            // barriers count both CTAs' loads.
+            if (rank == 0)
+                for (int i = 0; i < issued; i++)
+                    if (!ptx::mbar_wait(&full[i], i < stage ? phase : phase ^ 1, DRAIN_NS, nullptr))
+                        raise_abort(p, abort_flag, 4, peer_flag);
         }
     } else if (warp == 1) {
-        // ------------------------------------------------ MMA issuer
-        if (lane == 0) {
-            const uint32_t idesc = ptx::idesc_bf16_f32(kBM, kBN);
+        // ------------------------------------------------ MMA issuer (the even CTA of a pair)
+        if (lane == 0 && rank == 0) {
+            const uint32_t idesc = ptx::idesc_bf16_f32(kBM * CL, kBN);
             const uint32_t smem_base = ptx::smem_u32(smem), full_base = ptx::smem_u32(full);
-            // Descriptors of the three slots, fixed for the whole kernel: the issue
-            // loop below is unrolled over the slots so that none is recomputed.
-            const uint64_t da0 = ptx::smem_desc_sw128(smem_base), db0 = ptx::smem_desc_sw128(smem_base + 2 * A_BYTES);
-            const uint64_t da1 = ptx::smem_desc_sw128(smem_base + STAGE_BYTES),
-                           db1 = ptx::smem_desc_sw128(smem_base + STAGE_BYTES + 2 * A_BYTES);
-            const uint64_t da2 = ptx::smem_desc_sw128(smem_base + 2 * STAGE_BYTES),
-                           db2 = ptx::smem_desc_sw128(smem_base + 2 * STAGE_BYTES + 2 * A_BYTES);
+            // Descriptors of the slots, fixed for the whole kernel: the issue loop
+            // below is unrolled over the slots so that none is recomputed.
+            uint64_t da[STAGES], db[STAGES];
+#pragma unroll
+            for (int i = 0; i < STAGES; i++) {
+                da[i] = ptx::smem_desc_sw128(smem_base + i * STAGE_BYTES);
+                db[i] = ptx::smem_desc_sw128(smem_base + i * STAGE_BYTES + GROUP_KB * A_BYTES);
+            }
+            // The barriers a commit arrives on: this CTA's, and in a pair the peer's too.
+            auto commit = [&](uint64_t *bar) {
+                if (CL == 1) {
+                    ptx::mma_commit(bar);
+                } else {
+                    const uint32_t a = ptx::smem_u32(bar);
+                    ptx::mma_commit_pair(a);
+                    ptx::mma_commit_pair(ptx::mapa(a, 1));
+                }
+            };
             uint32_t phase = 0;
             int abuf = 0;
             uint32_t aphase = 0;
@@ -329,7 +401,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             int tile = cta0, d = 0, s = 0, g = 0, in_chunk = 0;
             int gpp = tile < total_tiles ? entry_nkb<GROUPED>(p, items, work, tile) / GROUP_KB : 0;
             auto close_chunk = [&]() {
-                ptx::mma_commit(&accf[abuf]);
+                commit(&accf[abuf]);
                 abuf ^= 1;
                 if (abuf == 0) aphase ^= 1;
                 in_chunk = 0;
@@ -342,7 +414,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const bool got_acc = ptx::mbar_wait(&acce[abuf], aphase ^ 1, p.timeout_ns, abort_flag);
                     if (p.prof) prof_add(p, kProfMmaWaitAcc, clock64() - ta);
                     if (!got_acc) {
-                        raise_abort(p, abort_flag, 2);
+                        raise_abort(p, abort_flag, 2, peer_flag);
                         return false;
                     }
                     dt = tmem + (uint32_t)(abuf * kBN);
@@ -352,17 +424,15 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const bool got_full = ptx::mbar_wait(&full[ST], phase, p.timeout_ns, abort_flag);
                     if (p.prof) prof_add(p, kProfMmaWaitFull, clock64() - tf);
                     if (!got_full) {
-                        raise_abort(p, abort_flag, 2);
+                        raise_abort(p, abort_flag, 2, peer_flag);
                         return false;
                     }
                 }
                 ptx::tc_fence_after();
-                const uint64_t da = ST == 0 ? da0 : (ST == 1 ? da1 : da2);
-                const uint64_t db = ST == 0 ? db0 : (ST == 1 ? db1 : db2);
                 const uint32_t nphase = ST == STAGES - 1 ? phase ^ 1 : phase;
-                ready = mma_group<2>(dt, da, db, idesc, in_chunk > 0 ? 1u : 0u,
-                                     full_base + (uint32_t)(((ST + 1) % STAGES) * 8), nphase);
-                ptx::mma_commit(&empty[ST]);
+                ready = mma_group<CL>(dt, da[ST], db[ST], idesc, in_chunk > 0 ? 1u : 0u,
+                                      full_base + (uint32_t)(((ST + 1) % STAGES) * 8), nphase);
+                commit(&empty[ST]);
                 phase = nphase;
                 if (++in_chunk == kChunkKB / GROUP_KB) close_chunk();
                 if (++g == gpp) {
@@ -380,14 +450,26 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
                 return true;
             };
-            static_assert(STAGES == 3, "the issue loop is unrolled over three slots");
+            // one pass over the ring's slots
+            auto ring = [&]() -> bool {
+                if (!step(std::integral_constant<int, 0>{})) return false;
+                if (!step(std::integral_constant<int, 1>{})) return false;
+                if (!step(std::integral_constant<int, 2>{})) return false;
+                if constexpr (STAGES == 4) {
+                    if (!step(std::integral_constant<int, 3>{})) return false;
+                }
+                return true;
+            };
+            static_assert(STAGES == 3 || STAGES == 4, "the issue loop is unrolled over three or four slots");
             if (gpp > 0)
-                while (step(std::integral_constant<int, 0>{}) && step(std::integral_constant<int, 1>{}) &&
-                       step(std::integral_constant<int, 2>{})) {
+                while (ring()) {
                 }
             // All issued MMAs must complete before TMEM is released.
-            ptx::mma_commit(done);
-            if (!ptx::mbar_wait(done, 0, DRAIN_NS, nullptr)) raise_abort(p, abort_flag, 5);
+            if (CL == 1)
+                ptx::mma_commit(done);
+            else
+                ptx::mma_commit_pair(ptx::smem_u32(done));
+            if (!ptx::mbar_wait(done, 0, DRAIN_NS, nullptr)) raise_abort(p, abort_flag, 5, peer_flag);
         }
     } else {
         // ------------------------------------------------ epilogue (warps 2..9)
@@ -527,7 +609,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (p.prof && ew == 0 && lane == 0) prof_add(p, kProfEpiWaitAcc, tw1 - tw);
                     w = __all_sync(0xffffffffu, w);
                     if (!w) {
-                        if (lane == 0) raise_abort(p, abort_flag, 3);
+                        if (lane == 0) raise_abort(p, abort_flag, 3, peer_flag);
                         ok = false;
                         break;
                     }
@@ -542,7 +624,12 @@ __global__ void __launch_bounds__(THREADS, 1)
                     }
                     ptx::tc_fence_before();
                     __syncwarp();
-                    if (lane == 0) ptx::mbar_arrive(&acce[abuf]);
+                    if (lane == 0) {
+                        if (CL == 1)
+                            ptx::mbar_arrive(&acce[abuf]);
+                        else
+                            ptx::mbar_arrive_cluster_relaxed(acce_lead + (uint32_t)(abuf * 8));
+                    }
                     abuf ^= 1;
                     if (abuf == 0) aphase ^= 1;
                     // Fold L into H every 64 chunks and at the end of each slice group,
@@ -587,7 +674,13 @@ __global__ void __launch_bounds__(THREADS, 1)
             const long long tfin = (p.prof && ew == 0 && lane == 0) ? clock64() : 0;
             finalize_cols(kBN / 2);
             __syncwarp();
-            const TileJob job = resolve<GROUPED>(p, items, work, tile);
+            const TileJob job = resolve<GROUPED, CL>(p, items, work, tile, rank);
+            if (!GROUPED && job.tid < 0) {
+                // the odd half of a pair's last row of tiles: rows past the output
+                ptx::tc_fence_before();
+                pend = false;
+                continue;
+            }
             const int64_t m = (int64_t)job.mt * kBM + row;
             const bool row_ok = m < job.M;
             int64_t rowOff = 0;
@@ -645,25 +738,6 @@ __global__ void __launch_bounds__(THREADS, 1)
             rowOffW[lane] = rowOff;
             rowOkW[lane] = row_ok ? 1 : 0;
             __syncwarp();
-#if EG_PREFETCH_C
-            // The pending tile's C is read during the next tile's chunks: ask for its
-            // lines in L2 now, so that those reads wait on L2, not on DRAM.
-            if (finish && !direct && !plain_store) {
-                const bool fast = job.mg->n > 0 && job.mg->s[2][job.mg->n - 1] == 1;
-                if (fast) {
-                    // C runs along the rows: a 128-byte line holds 16 of this warp's rows
-                    if (row_ok && (lane & 15) == 0)
-                        for (int c = 0; c < kBN / 2; c++)
-                            if (colExp[c] != INT_MAX)
-                                asm volatile("prefetch.global.L2 [%0];" ::"l"(job.C + rowOff + colOff[c]));
-                } else if (row_ok) {
-                    // C runs along the columns: a line holds 16 of this row's columns
-                    for (int c = 0; c < kBN / 2; c += 16)
-                        if (colExp[c] != INT_MAX)
-                            asm volatile("prefetch.global.L2 [%0];" ::"l"(job.C + rowOff + colOff[c]));
-                }
-            }
-#endif
             if (direct) {
                 // the same conversion and stores as finalize_cols, the sums read from TMEM
                 const bool rows_fast = job.mg->n > 0 && job.mg->s[2][job.mg->n - 1] == 1;
@@ -735,10 +809,13 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
 
     __syncthreads();
+    // A CTA of a pair leaves only when the peer is done too: the even CTA's MMAs
+    // read the odd CTA's shared memory, and both CTAs arrive on each other's barriers.
+    if (CL == 2) ptx::cluster_sync();
     if (p.prof && threadIdx.x == 0) prof_add(p, kProfTotal, clock64() - t_start);
     if (warp == 1) {
         ptx::tc_fence_after();
-        ptx::tmem_dealloc(tmem, TMEM_COLS);
+        ptx::tmem_dealloc<CL>(tmem, TMEM_COLS);
     }
 }
 
@@ -748,23 +825,80 @@ eg_status ensure_tc_attributes() {
     static std::once_flag once;
     static cudaError_t err = cudaSuccess;
     std::call_once(once, [] {
-        err = cudaFuncSetAttribute(k_tc_split_gemm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        err = cudaFuncSetAttribute(k_tc_split_gemm<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   Ring<1>::SMEM_BYTES);
         if (err == cudaSuccess)
-            err = cudaFuncSetAttribute(k_tc_split_gemm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+            err = cudaFuncSetAttribute(k_tc_split_gemm<true, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       Ring<1>::SMEM_BYTES);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(k_tc_split_gemm<false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       Ring<2>::SMEM_BYTES);
     });
     if (err != cudaSuccess) return cuda_fail(err, "cudaFuncSetAttribute(k_tc_split_gemm)");
     return EG_SUCCESS;
 }
 
+namespace {
+cudaLaunchConfig_t pair_config(int grid, cudaStream_t s, cudaLaunchAttribute *attr) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(THREADS);
+    cfg.dynamicSmemBytes = Ring<2>::SMEM_BYTES;
+    cfg.stream = s;
+    attr->id = cudaLaunchAttributeClusterDimension;
+    attr->val.clusterDim.x = 2;
+    attr->val.clusterDim.y = 1;
+    attr->val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cfg;
+}
+} // namespace
+
+int tc_pair_clusters() {
+    static std::once_flag once;
+    static int n = 0;
+    std::call_once(once, [] {
+        // CTA pairs only on request: on the CCD shapes they measure slower than
+        // single-CTA tiles (the epilogue, not operand delivery, bounds the kernel)
+        const char *env = std::getenv("EINSUMS_GB300_TC_PAIRS");
+        if (!env || env[0] != '1') return;
+        if (ensure_tc_attributes() != EG_SUCCESS) return;
+        cudaLaunchAttribute attr;
+        cudaLaunchConfig_t cfg = pair_config(num_sms(), nullptr, &attr);
+        int c = 0;
+        if (cudaOccupancyMaxActiveClusters(&c, (void *)k_tc_split_gemm<false, 2>, &cfg) == cudaSuccess) n = c;
+        cudaGetLastError();
+    });
+    return n;
+}
+
 eg_status launch_tc_gemm(const CUtensorMap &tmA, const CUtensorMap &tmB, const TcGemmParams &p, cudaStream_t s) {
     eg_status st = ensure_tc_attributes();
     if (st != EG_SUCCESS) return st;
+    if (p.pair) {
+        const int clusters = tc_pair_clusters();
+        if (clusters < 1) return fail(EG_ERROR_CUDA, "k_tc_split_gemm: CTA pairs are not available");
+        const int total = p.nbatch * ((p.mtiles + 1) / 2) * p.ntiles * p.ksplit;
+        if (total <= 0) return EG_SUCCESS;
+        const int grid = 2 * (total < clusters ? total : clusters);
+        cudaLaunchAttribute attr;
+        cudaLaunchConfig_t cfg = pair_config(grid, s, &attr);
+        {
+            LaunchScope ls_("k_tc_split_gemm", s);
+            const TcItem *no_items = nullptr;
+            const int4 *no_work = nullptr;
+            EG_CUDA(cudaLaunchKernelEx(&cfg, k_tc_split_gemm<false, 2>, tmA, tmB, p, no_items, no_work, 0));
+        }
+        EG_CHECK_LAUNCH("k_tc_split_gemm");
+        return EG_SUCCESS;
+    }
     const int total = p.nbatch * p.mtiles * p.ntiles * p.ksplit;
     if (total <= 0) return EG_SUCCESS;
     const int grid = total < num_sms() ? total : num_sms();
     {
         LaunchScope ls_("k_tc_split_gemm", s);
-        k_tc_split_gemm<false><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p, nullptr, nullptr, 0);
+        k_tc_split_gemm<false, 1><<<grid, THREADS, Ring<1>::SMEM_BYTES, s>>>(tmA, tmB, p, nullptr, nullptr, 0);
     }
     EG_CHECK_LAUNCH("k_tc_split_gemm");
     return EG_SUCCESS;
@@ -778,10 +912,16 @@ eg_status launch_tc_gemm_grouped(const CUtensorMap &tmA, const CUtensorMap &tmB,
     const int grid = ntiles_total < num_sms() ? ntiles_total : num_sms();
     {
         LaunchScope ls_("k_tc_split_gemm_grouped", s);
-        k_tc_split_gemm<true><<<grid, THREADS, SMEM_BYTES, s>>>(tmA, tmB, p, items, work, ntiles_total);
+        k_tc_split_gemm<true, 1><<<grid, THREADS, Ring<1>::SMEM_BYTES, s>>>(tmA, tmB, p, items, work, ntiles_total);
     }
     EG_CHECK_LAUNCH("k_tc_split_gemm_grouped");
     return EG_SUCCESS;
 }
 
 } // namespace eg::split
+
+extern "C" eg_status eg_tc_pair_clusters(int32_t *clusters) {
+    if (!clusters) return eg::fail(EG_ERROR_INVALID_ARGUMENT, "eg_tc_pair_clusters: NULL output");
+    *clusters = eg::split::tc_pair_clusters();
+    return EG_SUCCESS;
+}

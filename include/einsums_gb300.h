@@ -288,6 +288,12 @@ eg_status eg_stream_synchronize(void *stream);
 eg_status eg_measure_fp64_peak(double *dfma_tflops, double *dmma_tflops);
 eg_status eg_measure_fp64_peak_clock(double *dfma_tflops, double *dmma_tflops, double *probe_mhz);
 
+/* *clusters receives the number of two-CTA clusters the split-BF16 tensor kernel
+ * runs single contractions on (256x128 output tiles, cta_group::2 MMAs), or 0
+ * when it runs one CTA per 128x128 tile.  Pairs are used when the process
+ * starts with EINSUMS_GB300_TC_PAIRS=1.  No reference counterpart. */
+eg_status eg_tc_pair_clusters(int32_t *clusters);
+
 /* Kernel accounting.  eg_kernel_launches: kernels this library has launched in the
  * process.  With profiling on, every launch is bracketed by CUDA events on its own
  * stream; eg_profile_summary synchronises those events and writes one line

@@ -3,6 +3,8 @@
 Tolerance: relative Frobenius error <= 1e-10 at the default 5 slices, and the
 error reported for every slice count (3..6) must fall with the count and stay
 under the a-priori bound the library reports."""
+import os
+
 import numpy as np
 import pytest
 
@@ -188,6 +190,58 @@ def test_e2e_slab_pipeline_matches_whole_step(eg):
     for k in ("Wmnij", "Wmbej", "Wabef"):
         assert torch.equal(out[k], W[k].cpu()), k
     assert abs(float(out["E"]) - float(W["E"])) <= 1e-14 * max(1.0, abs(float(W["E"])))
+
+
+PAIR_CASES = [(300, 200, 256, 0.0), (260, 100, 2048, 0.0), (1000, 520, 384, 1.0), (128, 640, 512, 0.0)]
+
+
+def pair_cases():
+    """Runs PAIR_CASES in this process and returns the number of pair clusters
+    the tensor kernel used; raises on the first result that is not bit-exact."""
+    import ctypes
+    import einsums_gb300 as eg
+    from einsums_gb300 import _lib
+    from test_split_math import split_product_fast
+    for M, N, K, cp in PAIR_CASES:
+        rng = np.random.default_rng(M + K)
+        A = rng.standard_normal((M, K)) * np.exp2(rng.integers(-10, 10, size=(M, 1)))
+        B = rng.standard_normal((N, K))
+        ref = split_product_fast(A, B, 5)
+        C0 = rng.standard_normal((M, N))
+        C = cu(C0)
+        eg.einsum(cp, "ij", C, 1.0, "ik", cu(A), "jk", cu(B), precision="split_bf16", slices=5)
+        want = ref if cp == 0.0 else C0 + ref
+        assert np.array_equal(C.cpu().numpy().view(np.uint64), want.view(np.uint64)), (M, N, K, cp)
+        # C contiguous along the rows (the epilogue path that runs one thread per row)
+        Ct = torch.zeros((N, M), dtype=torch.float64, device="cuda")
+        eg.einsum(0.0, "ji", Ct, 1.0, "ik", cu(A), "jk", cu(B), precision="split_bf16", slices=5)
+        assert np.array_equal(Ct.cpu().numpy().T.copy().view(np.uint64), ref.view(np.uint64)), (M, N, K, "rows")
+    n = ctypes.c_int32(-1)
+    _lib.check(_lib.load().eg_tc_pair_clusters(ctypes.byref(n)))
+    return n.value
+
+
+def test_single_cta_tiles_are_the_exact_split_product(eg):
+    """Outputs of several 128-row tiles, odd tile counts and a K cut into slices
+    (260 x 100, K = 2048): bit for bit the CPU restatement of the scheme."""
+    assert pair_cases() == 0  # this process runs single-CTA tiles
+
+
+def test_pair_tiles_are_the_exact_split_product(eg):
+    """The same cases on CTA pairs (256x128 tiles, cta_group::2), in a process
+    started with EINSUMS_GB300_TC_PAIRS=1: an odd row-tile count leaves the
+    second CTA of the last pair past the rows (300 and 1000 rows)."""
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(here)
+    path = os.pathsep.join([root, os.path.join(root, "oracle"), here, os.environ.get("PYTHONPATH", "")])
+    env = dict(os.environ, EINSUMS_GB300_TC_PAIRS="1", PYTHONPATH=path)
+    code = "import test_gpu_split as t; print('pairs', t.pair_cases())"
+    r = subprocess.run([sys.executable, "-c", code], cwd=here, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    clusters = int(r.stdout.split("pairs")[-1])
+    assert clusters > 0, r.stdout
 
 
 @pytest.mark.parametrize("S,K", [(3, 300), (4, 257), (5, 1000), (5, 70), (6, 128)])

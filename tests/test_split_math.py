@@ -52,6 +52,30 @@ def split_product(A, B, S):
     return out
 
 
+def split_product_fast(A, B, S):
+    """split_product with the digit products summed in FP64 (exact while
+    K * 2^14 < 2^53) and the Horner combination in int64 (|R| < 2^62 for one
+    exact pass of K)."""
+    assert A.shape[1] * 2 ** 14 < 2 ** 53
+    eA, eB = exponents(A), exponents(B)
+    a, b = digits(A, eA, S), digits(B, eB, S)
+    R = np.zeros((A.shape[0], B.shape[0]), dtype=np.int64)
+    for d in range(S):
+        G = sum(a[s].astype(np.float64) @ b[d - s].T.astype(np.float64) for s in range(d + 1))
+        R = R * 256 + G.astype(np.int64)
+    shift = eA[:, None] + eB[None, :] - 2 * TOP - BITS * (S - 1)
+    return np.ldexp(R.astype(np.float64), shift.astype(np.int64))
+
+
+def test_fast_split_product_matches_exact_integers():
+    rng = np.random.default_rng(4)
+    A = rng.standard_normal((9, 150)) * np.exp2(rng.integers(-30, 30, size=(9, 1)))
+    B = rng.standard_normal((7, 150))
+    A[2] = 0.0
+    for S in (3, 5, 6):
+        assert np.array_equal(split_product(A, B, S).view(np.uint64), split_product_fast(A, B, S).view(np.uint64))
+
+
 @pytest.mark.parametrize("S", [2, 3, 4, 5, 6])
 def test_digits_are_bf16_exact_and_reconstruct(S):
     rng = np.random.default_rng(S)
