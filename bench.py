@@ -40,9 +40,9 @@ def flops(o, v):
 
 
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the tensor kernel on the
-# o=32, v=160 workload, mean over the step's three launches (Wmnij 1.59 GB,
-# Wabef 24.56 GB, Wmbej 8.27 GB).
-TC_TRAFFIC_O32_V160 = 11.47e9
+# o=32, v=160 workload, mean over the step's three launches (Wmnij 3.32 GB,
+# Wabef 18.17 GB, Wmbej 6.37 GB), from a separate capture of this workload.
+TC_TRAFFIC_O32_V160 = 9.29e9
 
 
 def tc_algorithmic_bytes(o, v, S):
@@ -168,26 +168,37 @@ def rel_err(x, ref):
     return float(num / den) if float(den) > 0 else float(num)
 
 
-def oracle_sample_check(T, W_fp64, o, v, rows=2):
-    """CPU-oracle values of a few rows of each W, against the GPU FP64 results."""
+def oracle_sample_check(T, Ws, rows=4):
+    """CPU-oracle values of the first `rows` rows of each W's increment (the contraction
+    term, C_prefactor 0), against the increment each GPU result in `Ws` (name -> W dict)
+    made: rows m < 4 of 32 (Wmnij, Wmbej) and a < 4 of 160 (Wabef), plus the energy."""
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     t = T["t"].cpu().numpy()
     g = T["g_oovv"].cpu().numpy()
-    out = {}
-    ref = T["g_oooo"][:rows].cpu().numpy().copy()
-    oracle.einsum("mnij", ref, 1.0, 0.25, "ijef", t, "mnef", np.ascontiguousarray(g[:rows]))
-    out["Wmnij"] = oracle.rel_fro(W_fp64["Wmnij"][:rows].cpu().numpy(), ref)
-    ref = T["g_vvvv"][:rows].cpu().numpy().copy()
-    oracle.einsum("abef", ref, 1.0, 0.25, "mnef", g, "mnab", np.ascontiguousarray(t[:, :, :rows]))
-    out["Wabef"] = oracle.rel_fro(W_fp64["Wabef"][:rows].cpu().numpy(), ref)
-    ref = T["g_ovvo"][:rows].cpu().numpy().copy()
-    oracle.einsum("mbej", ref, 1.0, -0.5, "jnfb", t, "mnef", np.ascontiguousarray(g[:rows]))
-    out["Wmbej"] = oracle.rel_fro(W_fp64["Wmbej"][:rows].cpu().numpy(), ref)
+    init = {"Wmnij": "g_oooo", "Wabef": "g_vvvv", "Wmbej": "g_ovvo"}
+    refs = {}
+    ref = np.zeros_like(T["g_oooo"][:rows].cpu().numpy())
+    oracle.einsum("mnij", ref, 0.0, 0.25, "ijef", t, "mnef", np.ascontiguousarray(g[:rows]))
+    refs["Wmnij"] = ref
+    ref = np.zeros_like(T["g_vvvv"][:rows].cpu().numpy())
+    oracle.einsum("abef", ref, 0.0, 0.25, "mnef", g, "mnab", np.ascontiguousarray(t[:, :, :rows]))
+    refs["Wabef"] = ref
+    ref = np.zeros_like(T["g_ovvo"][:rows].cpu().numpy())
+    oracle.einsum("mbej", ref, 0.0, -0.5, "jnfb", t, "mnef", np.ascontiguousarray(g[:rows]))
+    refs["Wmbej"] = ref
     e = np.zeros(())
     oracle.einsum("", e, 0.0, 0.25, "ijab", t, "ijab", g)
-    out["E"] = abs(float(W_fp64["E"].item()) - float(e)) / max(abs(float(e)), 1e-300)
+    out = {}
+    for name, W in Ws.items():
+        res = {}
+        for k, ref in refs.items():
+            got = (W[k][:rows] - T[init[k]][:rows]).cpu().numpy()
+            res[k] = oracle.rel_fro(got, ref)
+        res["E"] = abs(float(W["E"].item()) - float(e)) / max(abs(float(e)), 1e-300)
+        out[name] = res
+    out["rows"] = rows
     return out
 
 
@@ -314,6 +325,7 @@ def run_ours(args, rank, world):
     ccd_step(eg, T, W64, "fp64", 0)
     errors = {}
     split_report = None
+    checked = {"fp64": W64}
     if headline == "split_bf16":
         Ws = fresh_W(T)
         split_report = {}
@@ -321,9 +333,11 @@ def run_ours(args, rank, world):
         for k in ("Wmnij", "Wabef", "Wmbej"):
             errors[k] = rel_err(Ws[k] - T[{"Wmnij": "g_oooo", "Wabef": "g_vvvv", "Wmbej": "g_ovvo"}[k]],
                                 W64[k] - T[{"Wmnij": "g_oooo", "Wabef": "g_vvvv", "Wmbej": "g_ovvo"}[k]])
-        del Ws
+        checked["split_bf16"] = Ws
     torch.cuda.synchronize()
-    oracle_err = oracle_sample_check(T, W64, o, v) if rank == 0 else None
+    oracle_err = oracle_sample_check(T, checked) if rank == 0 else None
+    del checked
+    Ws = None
 
     def timed(precision, steps, warmup, timers=None):
         W = fresh_W(T)
@@ -403,10 +417,12 @@ def run_ours(args, rank, world):
                 # launches, from one ncu capture of this workload
                 # (dram__bytes_read.sum + dram__bytes_write.sum); algorithmic bytes
                 # per launch (digit planes read once, C read and written once) are
-                # 4.16 GB; the kernel moves 2.8x that (re-reads of digit-plane tiles
-                # evicted by the streamed output, and of the per-CTA sum scratch).
+                # 4.16 GB; the kernel moves 2.2x that (digit-plane panels re-read
+                # through L2 by the output tiles that share them).
                 roof["traffic"] = TC_TRAFFIC_O32_V160
-                roof["traffic_unit"] = "bytes per launch (ncu, mean of the step's 3 launches)"
+                roof["traffic_unit"] = ("bytes per launch, mean of the step's 3 launches, from an ncu capture of "
+                                        "this workload (profiles/k_tc_split_gemm_traffic_ccd_o32_v160.md), "
+                                        "not measured in this run")
                 roof["algorithmic_bytes"] = tc_algorithmic_bytes(o, v, 5)
         else:
             alg = F["Wabef"]
@@ -453,7 +469,7 @@ def run_ours(args, rank, world):
                            "fp64_probe_sm_mhz": probe_mhz.value},
             "split_vs_fp64_speedup": value / world / fp64_value if headline == "split_bf16" else None,
             "per_contraction_ms": per_contraction, "kernels": kernels, "kernels_steps": args.steps + args.warmup,
-            "error_vs_fp64": errors, "error_fp64_vs_oracle_sample": oracle_err, "split_report": split_report,
+            "error_vs_fp64": errors, "error_vs_oracle_sample": oracle_err, "split_report": split_report,
             "roofline": roof, "cpu_baseline": cpu, "clocks": clk.summary(), "e2e": e2e, "gpu_launches": launches,
             "suites": suites,
         }
@@ -726,7 +742,7 @@ def _graph_ms(fns):
     torch.cuda.current_stream().wait_stream(s)
     torch.cuda.synchronize()
     g = torch.cuda.CUDAGraph()
-    with torch.cuda.graph(g):
+    with torch.cuda.graph(g, stream=s):
         for fn in fns:
             fn()
     g.replay()
@@ -931,6 +947,24 @@ def suite_autograd(eg, o=24, v=96):
     return res
 
 
+def suite_gemm(eg, m=8192, k=1024, c_along_m=True, reps=3):
+    """One split-BF16 GEMM-shaped contraction C[b,a] (or C[a,b]) = sum_k A[a,k] B[b,k],
+    M = N = m: the Wabef shape at a chosen size, for timing the tensor kernel and for
+    profiling it on a case smaller than the CCD step.  Not part of the default line."""
+    import torch
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(m + k)
+    A = torch.randn((m, k), generator=gen, dtype=torch.float64, device="cuda")
+    B = torch.randn((m, k), generator=gen, dtype=torch.float64, device="cuda")
+    C = torch.zeros((m, m), dtype=torch.float64, device="cuda")
+    Cl = "ba" if c_along_m else "ab"
+    run = lambda: eg.einsum(1.0, Cl, C, 1.0, "ak", A, "bk", B, precision="split_bf16")
+    ms = _time(run, reps=reps, warm=1)
+    pairs = eg.last_split_report()["slice_pairs"]
+    return {"config": f"split-BF16 GEMM M=N={m} K={k}, C contiguous along {'M' if c_along_m else 'N'}",
+            "ms": ms, "bf16_tflops_incl_splitting": pairs * 2.0 * m * m * k / ms / 1e9}
+
+
 SUITES = ("fock", "permute", "contraction", "batched", "autograd")
 
 
@@ -966,6 +1000,9 @@ def run_suite(args):
             r = fns[name](eg, sizes)
         elif name == "batched" and args.items:
             r = fns[name](eg, count=args.items)
+        elif name == "gemm":
+            mk = sizes or (8192, 1024)
+            r = fns[name](eg, m=mk[0], k=mk[1], reps=args.steps)
         else:
             r = fns[name](eg)
         r["suite"] = name
@@ -974,7 +1011,7 @@ def run_suite(args):
 
 
 SUITE_FNS = {"fock": suite_fock, "permute": suite_permute, "contraction": suite_contraction, "batched": suite_batched,
-             "autograd": suite_autograd}
+             "autograd": suite_autograd, "gemm": suite_gemm}
 
 
 def main():
@@ -992,7 +1029,8 @@ def main():
                     help="skip the other configurations that follow the headline in the same line")
     ap.add_argument("--suite", default=None,
                     help="measure the other configurations instead (all, or a comma list of "
-                         "fock,permute,contraction,batched,autograd); one JSON line each")
+                         "fock,permute,contraction,batched,autograd; gemm: one split-form GEMM of "
+                         "--sizes M,K, --steps calls); one JSON line each")
     ap.add_argument("--sizes", default=None, help="extents for the permute / contraction sweeps, e.g. 64,128")
     ap.add_argument("--items", type=int, default=0, help="contractions in the batched suite (default 2048)")
     args = ap.parse_args()

@@ -115,16 +115,37 @@ std::mutex &g_status_mutex = *new std::mutex;
 std::map<WsKey, int *> &g_status = *new std::map<WsKey, int *>;
 } // namespace
 
+// One status word per (device, stream), allocated on first use.  A stream that
+// is being captured into a CUDA graph cannot allocate: it gets its own word if
+// one exists, else the device's shared word for captured launches (created with
+// the first word of the device, outside any capture).
 eg_status status_word(cudaStream_t stream, int **ptr) {
     int dev = 0;
     EG_CUDA(cudaGetDevice(&dev));
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    EG_CUDA(cudaStreamIsCapturing(stream, &cap));
     std::lock_guard<std::mutex> lk(g_status_mutex);
-    int *&w = g_status[WsKey{dev, stream}];
-    if (!w) {
-        EG_CUDA(cudaMalloc(&w, 256));
-        EG_CUDA(cudaMemset(w, 0, 256));
+    const WsKey shared_key{dev, reinterpret_cast<cudaStream_t>(~uintptr_t(0))};
+    auto found = g_status.find(WsKey{dev, stream});
+    if (found != g_status.end() && found->second) {
+        *ptr = found->second;
+        return EG_SUCCESS;
     }
-    *ptr = w;
+    if (cap != cudaStreamCaptureStatusNone) {
+        auto sh = g_status.find(shared_key);
+        if (sh == g_status.end() || !sh->second)
+            return fail(EG_ERROR_NOT_SUPPORTED, "first call of the library on this device is under stream capture");
+        *ptr = sh->second;
+        return EG_SUCCESS;
+    }
+    for (const WsKey &key : {shared_key, WsKey{dev, stream}}) {
+        int *&w = g_status[key];
+        if (!w) {
+            EG_CUDA(cudaMalloc(&w, 256));
+            EG_CUDA(cudaMemset(w, 0, 256));
+        }
+    }
+    *ptr = g_status[WsKey{dev, stream}];
     return EG_SUCCESS;
 }
 

@@ -671,10 +671,11 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     }
     p.status = status;
     p.timeout_ns = 2000ull * 1000 * 1000;
+    p.d0 = 0; // every slice group in one launch (K fits one exact pass)
+    p.d1 = S;
     p.ksplit = 1; // no K slicing in grouped launches
     p.kslice = 0;
-    static const bool shared_maps = std::getenv("EINSUMS_GB300_GROUPED_SHARED_MAPS") != nullptr;
-    p.item_maps = shared_maps ? nullptr : (const CUtensorMap *)d_maps;
+    p.item_maps = (const CUtensorMap *)d_maps;
     p.rbuf = (long long *)rbuf;
     static const bool prof_on = std::getenv("EINSUMS_GB300_TC_PROFILE") != nullptr;
     if (prof_on) {

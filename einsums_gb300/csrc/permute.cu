@@ -15,9 +15,11 @@
 // Arithmetic follows HPTT, the reference's host transposer: cp == 0 stores
 // ap*A without reading C (a plain copy when ap == 1, so the copy is bit-exact),
 // otherwise ap*A + cp*C without fused multiply-adds.
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
+#include "ptx.cuh"
 
 namespace eg {
 eg_status build_permute_desc(double cp, const int32_t *Cl, const eg_tensor *C, double ap, const int32_t *Al,
@@ -138,7 +140,165 @@ __global__ void __launch_bounds__(TILE *ROWS) k_permute_tiles(PermuteMap rest, i
     }
 }
 
+// ---------------------------------------------------------------- TMA tiles --
+// The transposing case through the tensor-memory accelerator: a 32x32 box of A
+// (A's fastest mode x C's fastest mode, plus one index of every other mode) is
+// loaded into shared memory, transposed there, and the 32x32 box of C is
+// stored back with one bulk tensor store.  Tiles at the edges are clipped by
+// the hardware (zero fill on load, bounds on store).  A ring of kTmaStages
+// slots keeps the loads of later tiles in flight while a tile is transposed;
+// a slot's output buffer is reused only after its store has read it.
+constexpr int kTmaTile = 32, kTmaStages = 4, kTmaThreads = 256;
+constexpr int kTmaBoxBytes = kTmaTile * kTmaTile * 8;
+constexpr int kTmaSmem = 2 * kTmaStages * kTmaBoxBytes + 128 + 1024;
+constexpr unsigned long long kTmaWaitNs = 2000ull * 1000 * 1000;
+
+struct TmaPermute {
+    int rank = 0;                  // tensor-map rank: 2 + rest modes (at most 5)
+    uint32_t tilesA = 0, tilesC = 0, total = 0; // total < 2^31
+    uint32_t rext[3] = {1, 1, 1};  // extents of the rest modes (slowest first)
+};
+
+template <int R>
+__device__ __forceinline__ void tma_load(void *dst, const CUtensorMap *m, uint64_t *bar, const int (&c)[5]) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst), b = (uint32_t)__cvta_generic_to_shared(bar);
+    const uint64_t mp = reinterpret_cast<uint64_t>(m);
+    if constexpr (R == 2)
+        asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+                     "%4}], [%2];" ::"r"(d), "l"(mp), "r"(b), "r"(c[0]), "r"(c[1])
+                     : "memory");
+    else if constexpr (R == 3)
+        asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+                     "%4, %5}], [%2];" ::"r"(d), "l"(mp), "r"(b), "r"(c[0]), "r"(c[1]), "r"(c[2])
+                     : "memory");
+    else if constexpr (R == 4)
+        asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+                     "%4, %5, %6}], [%2];" ::"r"(d), "l"(mp), "r"(b), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3])
+                     : "memory");
+    else
+        asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+                     "%4, %5, %6, %7}], [%2];" ::"r"(d), "l"(mp), "r"(b), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]),
+                     "r"(c[4])
+                     : "memory");
+}
+
+template <int R>
+__device__ __forceinline__ void tma_store(const CUtensorMap *m, const void *src, const int (&c)[5]) {
+    const uint32_t sp = (uint32_t)__cvta_generic_to_shared(src);
+    const uint64_t mp = reinterpret_cast<uint64_t>(m);
+    if constexpr (R == 2)
+        asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(mp), "r"(sp),
+                     "r"(c[0]), "r"(c[1])
+                     : "memory");
+    else if constexpr (R == 3)
+        asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(mp),
+                     "r"(sp), "r"(c[0]), "r"(c[1]), "r"(c[2])
+                     : "memory");
+    else if constexpr (R == 4)
+        asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(mp),
+                     "r"(sp), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3])
+                     : "memory");
+    else
+        asm volatile("cp.async.bulk.tensor.5d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5, %6}], [%1];" ::"l"(
+                         mp),
+                     "r"(sp), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4])
+                     : "memory");
+}
+
+// Box coordinates of tile t: {A-fast, C-fast, rest...} for the load and
+// {C-fast, A-fast, rest...} for the store (32-bit arithmetic: one thread issues
+// every copy of the CTA, so this sits on its critical path).
+__device__ __forceinline__ void tma_tile_coords(const TmaPermute &tp, uint32_t t, int (&ca)[5], int (&cc)[5]) {
+    uint32_t q = t / tp.tilesC;
+    const uint32_t tc = t - q * tp.tilesC;
+    t = q;
+    q = t / tp.tilesA;
+    const uint32_t ta = t - q * tp.tilesA;
+    t = q;
+    ca[0] = cc[1] = (int)(ta * kTmaTile);
+    ca[1] = cc[0] = (int)(tc * kTmaTile);
+#pragma unroll
+    for (int d = 2; d >= 0; d--) { // rest modes, fastest last; map dims 2.. hold them slowest last
+        q = tp.rext[d] == 1 ? t : t / tp.rext[d];
+        ca[2 + d] = cc[2 + d] = (int)(t - q * tp.rext[d]);
+        t = q;
+    }
+}
+
+template <int R, int MODE>
+__global__ void __launch_bounds__(kTmaThreads) k_permute_tma(const __grid_constant__ CUtensorMap mapA,
+                                                             const __grid_constant__ CUtensorMap mapC, TmaPermute tp,
+                                                             double ap, int *status) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    double *in = (double *)smem;                                  // [stage][C-fast j][A-fast i]
+    double *out = (double *)(smem + kTmaStages * kTmaBoxBytes);   // [stage][A-fast i][C-fast j]
+    uint64_t *full = (uint64_t *)(smem + 2 * kTmaStages * kTmaBoxBytes);
+    volatile int *abort_flag = (volatile int *)(full + kTmaStages);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) {
+        for (int i = 0; i < kTmaStages; i++) ptx::mbar_init(&full[i], 1);
+        *abort_flag = 0;
+        ptx::fence_mbar_init();
+        ptx::tma_prefetch_desc(&mapA);
+        ptx::tma_prefetch_desc(&mapC);
+    }
+    __syncthreads();
+    const uint32_t first = blockIdx.x, step = gridDim.x;
+    auto issue_load = [&](uint32_t k) { // local tile k of this CTA into slot k % stages
+        const uint32_t t = first + k * step;
+        if (t >= tp.total) return;
+        int ca[5], cc[5];
+        tma_tile_coords(tp, t, ca, cc);
+        uint64_t *bar = &full[k % kTmaStages];
+        ptx::mbar_arrive_expect_tx(bar, (uint32_t)kTmaBoxBytes);
+        tma_load<R>(in + (k % kTmaStages) * kTmaTile * kTmaTile, &mapA, bar, ca);
+    };
+    if (tid == 0)
+        for (uint32_t k = 0; k < kTmaStages; k++) issue_load(k);
+    int st_c[5] = {0, 0, 0, 0, 0}; // thread 0: the store coordinates of the current tile
+    for (uint32_t k = 0; first + k * step < tp.total; k++) {
+        const int slot = (int)(k % kTmaStages);
+        const uint32_t parity = (k / kTmaStages) & 1u;
+        if (tid == 0) {
+            int ca[5];
+            tma_tile_coords(tp, first + k * step, ca, st_c);
+        }
+        if (!ptx::mbar_wait(&full[slot], parity, kTmaWaitNs, abort_flag)) {
+            *abort_flag = 1;
+            atomicCAS(status, 0, 6);
+        }
+        if (tid == 0) // the store that last read this slot's output buffer has finished reading
+            asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(kTmaStages - 1) : "memory");
+        __syncthreads();
+        if (*abort_flag) break;
+        const double *src = in + slot * kTmaTile * kTmaTile;
+        double *dst = out + slot * kTmaTile * kTmaTile;
+        // lane l moves element (j = l, i = (l + c) mod 32): both the read of row j
+        // and the write of row i touch 16 distinct 8-byte bank pairs per half-warp
+#pragma unroll
+        for (int c = warp; c < kTmaTile; c += kTmaThreads / 32) {
+            const int j = lane, i = (lane + c) & (kTmaTile - 1);
+            const double v = src[j * kTmaTile + i];
+            dst[i * kTmaTile + j] = MODE == 0 ? v : __dmul_rn(ap, v);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            tma_store<R>(&mapC, dst, st_c);
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        } else if (tid == 32) {
+            issue_load(k + kTmaStages); // this slot's input buffer was read by every thread above
+        }
+    }
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    __syncthreads();
+}
+
 } // namespace
+
+eg_status encode_tiled_f64(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
+                           const uint64_t *strides_bytes, const uint32_t *box);
 
 // What a permute launch needs, fixed by the shapes and strides alone: a
 // compiled plan keeps it and runs it on new pointers.
@@ -151,6 +311,11 @@ struct PermuteLaunch {
     int64_t L = 0, sa = 0, sc = 0;                                 // rows
     int64_t EA = 0, EC = 0, saA = 0, scA = 0, saC = 0, scC = 0; // tiles
     double ap = 1.0, cp = 0.0;
+    // TMA form of the tiled case (cp == 0, fastest strides 1, other strides
+    // multiples of 16 bytes, at most three other modes); maps are encoded per run
+    bool tma = false;
+    TmaPermute tp;
+    int64_t rsA[3] = {}, rsC[3] = {}; // strides of the other modes (elements)
 };
 
 PermuteLaunch prepare_permute(const PermuteDesc &p) {
@@ -218,11 +383,122 @@ PermuteLaunch prepare_permute(const PermuteDesc &p) {
     const int64_t work =
         pl.rest.total * ((pl.EA + TILE - 1) / TILE) * (((pl.EC + TILE - 1) / TILE + kStrip - 1) / kStrip);
     pl.grid = (int)(work < cap ? work : cap);
+    // the TMA form: a plain or scaled copy of whole 32x32 boxes along two
+    // contiguous fastest modes, the other strides 16-byte multiples
+    bool ok = pl.mode <= 1 && pl.rest.n <= 3 && pl.saA == 1 && pl.scC == 1 && pl.EA >= kTmaTile &&
+              pl.EC >= kTmaTile && pl.EA < (1ll << 31) && pl.EC < (1ll << 31) && pl.saC % 2 == 0 && pl.scA % 2 == 0;
+    for (int d = 0; d < pl.rest.n && ok; d++)
+        ok = pl.rest.sA[d] % 2 == 0 && pl.rest.sC[d] % 2 == 0 && pl.rest.ext[d] < (1ll << 31);
+    if (ok) {
+        pl.tma = true;
+        pl.tp.rank = 2 + pl.rest.n;
+        pl.tp.tilesA = (uint32_t)((pl.EA + kTmaTile - 1) / kTmaTile);
+        pl.tp.tilesC = (uint32_t)((pl.EC + kTmaTile - 1) / kTmaTile);
+        const int64_t total = pl.rest.total * (int64_t)pl.tp.tilesA * pl.tp.tilesC;
+        pl.tma = total < (1ll << 31);
+        pl.tp.total = (uint32_t)total;
+        for (int d = 0; d < pl.rest.n; d++) {
+            pl.tp.rext[d] = (uint32_t)pl.rest.ext[d];
+            pl.rsA[d] = pl.rest.sA[d];
+            pl.rsC[d] = pl.rest.sC[d];
+        }
+    }
     return pl;
 }
 
+namespace {
+template <int MODE>
+eg_status launch_tma(const PermuteLaunch &pl, int grid, const CUtensorMap &mA, const CUtensorMap &mC, int *status,
+                     cudaStream_t s) {
+    switch (pl.tp.rank) {
+    case 2: k_permute_tma<2, MODE><<<grid, kTmaThreads, kTmaSmem, s>>>(mA, mC, pl.tp, pl.ap, status); break;
+    case 3: k_permute_tma<3, MODE><<<grid, kTmaThreads, kTmaSmem, s>>>(mA, mC, pl.tp, pl.ap, status); break;
+    case 4: k_permute_tma<4, MODE><<<grid, kTmaThreads, kTmaSmem, s>>>(mA, mC, pl.tp, pl.ap, status); break;
+    default: k_permute_tma<5, MODE><<<grid, kTmaThreads, kTmaSmem, s>>>(mA, mC, pl.tp, pl.ap, status); break;
+    }
+    return EG_SUCCESS;
+}
+
+eg_status ensure_tma_attributes() {
+    static std::once_flag once;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [] {
+        auto set = [&](const void *f) {
+            if (err == cudaSuccess) err = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmaSmem);
+        };
+        set((const void *)k_permute_tma<2, 0>);
+        set((const void *)k_permute_tma<3, 0>);
+        set((const void *)k_permute_tma<4, 0>);
+        set((const void *)k_permute_tma<5, 0>);
+        set((const void *)k_permute_tma<2, 1>);
+        set((const void *)k_permute_tma<3, 1>);
+        set((const void *)k_permute_tma<4, 1>);
+        set((const void *)k_permute_tma<5, 1>);
+    });
+    if (err != cudaSuccess) return cuda_fail(err, "cudaFuncSetAttribute(k_permute_tma)");
+    return EG_SUCCESS;
+}
+
+// Resident CTAs of the TMA permute per SM (its ring takes 65 KB of shared memory).
+int tma_blocks_per_sm() {
+    static std::once_flag once;
+    static int per_sm = 1;
+    std::call_once(once, [] {
+        int n = 0;
+        if (ensure_tma_attributes() == EG_SUCCESS &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_permute_tma<4, 0>, kTmaThreads, kTmaSmem) ==
+                cudaSuccess &&
+            n > 0)
+            per_sm = n;
+        cudaGetLastError();
+    });
+    return per_sm;
+}
+
+// Encodes the two maps for these pointers and launches; EG_ERROR_NOT_SUPPORTED
+// (nothing launched) when the pointers or the driver reject the TMA form.
+eg_status run_permute_tma(const PermuteLaunch &pl, const double *A, double *C, cudaStream_t s) {
+    if (((uintptr_t)A & 15) || ((uintptr_t)C & 15)) return EG_ERROR_NOT_SUPPORTED;
+    const int R = pl.tp.rank;
+    uint64_t dA[5], dC[5], sA[4], sC[4];
+    uint32_t box[5] = {kTmaTile, kTmaTile, 1, 1, 1};
+    dA[0] = (uint64_t)pl.EA;
+    dA[1] = (uint64_t)pl.EC;
+    sA[0] = (uint64_t)pl.saC * 8;
+    dC[0] = (uint64_t)pl.EC;
+    dC[1] = (uint64_t)pl.EA;
+    sC[0] = (uint64_t)pl.scA * 8;
+    for (int d = 0; d + 2 < R; d++) {
+        dA[2 + d] = dC[2 + d] = (uint64_t)pl.tp.rext[d];
+        sA[1 + d] = (uint64_t)pl.rsA[d] * 8;
+        sC[1 + d] = (uint64_t)pl.rsC[d] * 8;
+    }
+    CUtensorMap mA, mC;
+    if (encode_tiled_f64(&mA, A, R, dA, sA, box) != EG_SUCCESS) return EG_ERROR_NOT_SUPPORTED;
+    if (encode_tiled_f64(&mC, C, R, dC, sC, box) != EG_SUCCESS) return EG_ERROR_NOT_SUPPORTED;
+    set_error("");
+    eg_status st = ensure_tma_attributes();
+    if (st != EG_SUCCESS) return st;
+    int *status = nullptr;
+    if ((st = status_word(s, &status)) != EG_SUCCESS) return st;
+    const int64_t slots = (int64_t)tma_blocks_per_sm() * num_sms();
+    const int grid = (int)(pl.tp.total < slots ? pl.tp.total : slots);
+    {
+        LaunchScope ls_("k_permute_tma", s);
+        st = pl.mode == 0 ? launch_tma<0>(pl, grid, mA, mC, status, s) : launch_tma<1>(pl, grid, mA, mC, status, s);
+    }
+    if (st != EG_SUCCESS) return st;
+    EG_CHECK_LAUNCH("k_permute_tma");
+    return EG_SUCCESS;
+}
+} // namespace
+
 eg_status run_permute(const PermuteLaunch &pl, const double *A, double *C, cudaStream_t s) {
     if (pl.empty) return EG_SUCCESS;
+    if (pl.tma) {
+        const eg_status st = run_permute_tma(pl, A, C, s);
+        if (st != EG_ERROR_NOT_SUPPORTED) return st;
+    }
     if (pl.rows) {
         {
             LaunchScope ls_("k_permute_rows", s);

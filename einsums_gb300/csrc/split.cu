@@ -364,6 +364,27 @@ eg_status encode_planes_public(CUtensorMap *map, void *base, int64_t Kp, int64_t
     return split::encode_planes(map, base, Kp, rows, planes);
 }
 
+// A tiled map over an FP64 tensor of rank 2..5: dims[0] is the contiguous mode,
+// strides_bytes[i] the byte stride of mode i + 1, no swizzle, zero fill.
+eg_status encode_tiled_f64(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
+                           const uint64_t *strides_bytes, const uint32_t *box) {
+    auto fn = split::encode_fn();
+    if (!fn) return fail(EG_ERROR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    cuuint64_t d[5], st[4];
+    cuuint32_t b[5], es[5];
+    for (int i = 0; i < rank; i++) {
+        d[i] = dims[i];
+        b[i] = box[i];
+        es[i] = 1;
+        if (i + 1 < rank) st[i] = strides_bytes[i];
+    }
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, (cuuint32_t)rank, const_cast<void *>(base), d, st, b, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(EG_ERROR_NOT_SUPPORTED, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return EG_SUCCESS;
+}
+
 // A map over `planes` planes of `rows` x `K` BF16 digits laid out with row
 // stride Kp and plane stride Rp * Kp elements (the extents may be below the
 // padded layout: TMA then fills the rest of a box with zeros).
@@ -467,69 +488,88 @@ eg_status launch_split_contract(const Contraction &c, int slices, cudaStream_t s
     p.racc = kslicing ? (long long *)(base + offRacc) : nullptr;
     p.rcnt = kslicing ? (int *)(base + offRcnt) : nullptr;
 
-    // K passes small enough for the exact int64 accumulator; later passes add into C.
-    const int64_t kpass = max_k_per_pass(S);
+    // Launches: when all slice groups' exact sum fits int64 over the whole K (up to
+    // 65024 for S = 5), one.  Otherwise the slice groups are cut into ranges whose
+    // own exact sums fit (S = 6 with K = 16384: groups 0-4 and 5), each range added
+    // into C in FP64 by its own launch -- one extra rounding per range instead of a
+    // launch (and a read and write of C) per 128 of K; a range that still cannot
+    // take the whole K runs K passes.
     const int64_t nkb_total = Kp / kBK;
-    const int64_t kb_per_pass = kpass / kBK;
-    if (kb_per_pass < 1) return fail(EG_ERROR_NOT_SUPPORTED, "split form: slice count too large for exact accumulation");
-    for (int64_t kb0 = 0; kb0 < nkb_total || kb0 == 0; kb0 += kb_per_pass) {
-        p.kb0 = (int)kb0;
-        p.nkb = (int)std::min<int64_t>(kb_per_pass, nkb_total - kb0);
-        // slices of at least 16 K blocks (one exact chunk); the count minimises the
-        // estimated makespan: rounds of work entries over the SMs times the K blocks
-        // of one entry, plus about four blocks' worth of per-entry epilogue work
-        p.ksplit = 1;
-        p.kslice = p.nkb;
-        if (kslicing && p.nkb >= 32) {
-            // schedule units: tiles over SMs, or pair tiles over CTA pairs
-            const int64_t units = pair ? nb * ((Mp / kBM + 1) / 2) * (Np / kBN) : tiles;
-            const int64_t workers = pair ? clusters : num_sms();
-            int64_t best = -1;
-            for (int ks = 1; ks <= p.nkb / 16; ks++) {
-                const int64_t slice = round_up((p.nkb + ks - 1) / ks, kKStep / kBK);
-                const int64_t n = (p.nkb + slice - 1) / slice; // slices actually used
-                const int64_t rounds = (units * n + workers - 1) / workers;
-                const int64_t cost = rounds * (slice + 4);
-                if (best < 0 || cost < best) {
-                    best = cost;
-                    p.kslice = (int)slice;
-                    p.ksplit = (int)n;
+    std::vector<std::pair<int, int>> ranges;
+    for (int d0 = 0; d0 < S;) {
+        int d1 = d0 + 1;
+        while (d1 < S && max_k_per_pass_groups(d0, d1 + 1) >= Kp) d1++;
+        ranges.push_back({d0, d1});
+        d0 = d1;
+    }
+    const int shift_base = p.shift_const;
+    bool first_launch = true;
+    for (const auto &range : ranges) {
+        p.d0 = range.first;
+        p.d1 = range.second;
+        p.shift_const = shift_base + kBits * (S - p.d1);
+        const int64_t kb_per_pass = max_k_per_pass_groups(p.d0, p.d1) / kBK;
+        if (kb_per_pass < 1) return fail(EG_ERROR_NOT_SUPPORTED, "split form: slice count too large for exact accumulation");
+        for (int64_t kb0 = 0; kb0 < nkb_total || kb0 == 0; kb0 += kb_per_pass) {
+            p.kb0 = (int)kb0;
+            p.nkb = (int)std::min<int64_t>(kb_per_pass, nkb_total - kb0);
+            // slices of at least 16 K blocks (one exact chunk); the count minimises the
+            // estimated makespan: rounds of work entries over the SMs times the K blocks
+            // of one entry, plus about four blocks' worth of per-entry epilogue work
+            p.ksplit = 1;
+            p.kslice = p.nkb;
+            if (kslicing && p.nkb >= 32) {
+                // schedule units: tiles over SMs, or pair tiles over CTA pairs
+                const int64_t units = pair ? nb * ((Mp / kBM + 1) / 2) * (Np / kBN) : tiles;
+                const int64_t workers = pair ? clusters : num_sms();
+                int64_t best = -1;
+                for (int ks = 1; ks <= p.nkb / 16; ks++) {
+                    const int64_t slice = round_up((p.nkb + ks - 1) / ks, kKStep / kBK);
+                    const int64_t n = (p.nkb + slice - 1) / slice; // slices actually used
+                    const int64_t rounds = (units * n + workers - 1) / workers;
+                    const int64_t cost = rounds * (slice + 4);
+                    if (best < 0 || cost < best) {
+                        best = cost;
+                        p.kslice = (int)slice;
+                        p.ksplit = (int)n;
+                    }
                 }
             }
-        }
-        if (p.ksplit > 1) {
-            EG_CUDA(cudaMemsetAsync(p.racc, 0, raccBytes, s));
-            EG_CUDA(cudaMemsetAsync(p.rcnt, 0, rcntBytes, s));
-        }
-        const bool first = kb0 == 0;
-        p.cp = first ? c.cp : 1.0;
-        p.zero = first ? (c.zero_when_cp_zero ? 1 : 0) : 0;
-        if (p.nkb <= 0) break;
-        static const bool prof_on = std::getenv("EINSUMS_GB300_TC_PROFILE") != nullptr;
-        unsigned long long *prof = nullptr;
-        if (prof_on) {
-            EG_CUDA(cudaMalloc(&prof, (size_t)num_sms() * 8 * sizeof(unsigned long long)));
-            EG_CUDA(cudaMemsetAsync(prof, 0, (size_t)num_sms() * 8 * sizeof(unsigned long long), s));
-        }
-        p.prof = prof;
-        if ((st = launch_tc_gemm(tmA, tmB, p, s)) != EG_SUCCESS) return st;
-        if (prof) {
-            // Per-role wait/busy cycles summed over CTAs (a tracing aid, off by default).
-            std::vector<unsigned long long> h((size_t)num_sms() * 8);
-            EG_CUDA(cudaMemcpyAsync(h.data(), prof, h.size() * 8, cudaMemcpyDeviceToHost, s));
-            EG_CUDA(cudaStreamSynchronize(s));
-            cudaFree(prof);
-            double tot[8] = {0};
-            int ran = 0; // CTAs of the launch (its grid may be below the SM count)
-            for (size_t i = 0; i < h.size(); i++) tot[i % 8] += (double)h[i];
-            for (size_t i = 6; i < h.size(); i += 8) ran += h[i] > 0 ? 1 : 0;
-            std::fprintf(stderr,
-                         "[tc profile] M=%lld N=%lld K=%lld tiles=%d: total %.3g cyc/CTA | producer wait empty %.1f%% | "
-                         "mma wait full %.1f%% | mma wait acc %.1f%% | epi wait acc %.1f%% | epi flush %.1f%% | "
-                         "epi final %.1f%%\n",
-                         (long long)M, (long long)N, (long long)K, p.mtiles * p.ntiles * p.nbatch,
-                         tot[6] / (ran > 0 ? ran : 1), 100 * tot[0] / tot[6], 100 * tot[1] / tot[6], 100 * tot[2] / tot[6],
-                         100 * tot[3] / tot[6], 100 * tot[4] / tot[6], 100 * tot[5] / tot[6]);
+            if (p.ksplit > 1) {
+                EG_CUDA(cudaMemsetAsync(p.racc, 0, raccBytes, s));
+                EG_CUDA(cudaMemsetAsync(p.rcnt, 0, rcntBytes, s));
+            }
+            const bool first = first_launch;
+            first_launch = false;
+            p.cp = first ? c.cp : 1.0;
+            p.zero = first ? (c.zero_when_cp_zero ? 1 : 0) : 0;
+            if (p.nkb <= 0) break;
+            static const bool prof_on = std::getenv("EINSUMS_GB300_TC_PROFILE") != nullptr;
+            unsigned long long *prof = nullptr;
+            if (prof_on) {
+                EG_CUDA(cudaMalloc(&prof, (size_t)num_sms() * 8 * sizeof(unsigned long long)));
+                EG_CUDA(cudaMemsetAsync(prof, 0, (size_t)num_sms() * 8 * sizeof(unsigned long long), s));
+            }
+            p.prof = prof;
+            if ((st = launch_tc_gemm(tmA, tmB, p, s)) != EG_SUCCESS) return st;
+            if (prof) {
+                // Per-role wait/busy cycles summed over CTAs (a tracing aid, off by default).
+                std::vector<unsigned long long> h((size_t)num_sms() * 8);
+                EG_CUDA(cudaMemcpyAsync(h.data(), prof, h.size() * 8, cudaMemcpyDeviceToHost, s));
+                EG_CUDA(cudaStreamSynchronize(s));
+                cudaFree(prof);
+                double tot[8] = {0};
+                int ran = 0; // CTAs of the launch (its grid may be below the SM count)
+                for (size_t i = 0; i < h.size(); i++) tot[i % 8] += (double)h[i];
+                for (size_t i = 6; i < h.size(); i += 8) ran += h[i] > 0 ? 1 : 0;
+                std::fprintf(stderr,
+                             "[tc profile] M=%lld N=%lld K=%lld tiles=%d: total %.3g cyc/CTA | producer wait empty %.1f%% | "
+                             "mma wait full %.1f%% | mma wait acc %.1f%% | epi wait acc %.1f%% | epi flush %.1f%% | "
+                             "epi final %.1f%%\n",
+                             (long long)M, (long long)N, (long long)K, p.mtiles * p.ntiles * p.nbatch,
+                             tot[6] / (ran > 0 ? ran : 1), 100 * tot[0] / tot[6], 100 * tot[1] / tot[6], 100 * tot[2] / tot[6],
+                             100 * tot[3] / tot[6], 100 * tot[4] / tot[6], 100 * tot[5] / tot[6]);
+            }
         }
     }
     if (rep) {

@@ -19,6 +19,8 @@
 // Yokota (IJHPCA 2024), with BF16 digits and FP32 accumulation.
 #pragma once
 
+#include <climits>
+
 #include <cuda.h>
 
 #include "common.cuh"
@@ -67,6 +69,10 @@ struct TcGemmParams {
     // Launch as CTA pairs (cta_group::2, 256x128 tiles; B's tensor map has
     // 64-row boxes): single contractions only.
     int pair;
+    // Slice groups d0 <= d < d1 (anti-diagonals s + t = d of the digit pairs)
+    // summed by this launch: all of them (0, S) unless a long K is split into
+    // group ranges whose exact sums each fit int64 (finished into C one by one).
+    int d0, d1;
     // Grouped launches: two tensor maps per item (A, B) over the item's own digit
     // planes with its own row and K extents, so that TMA fills the tile's rows
     // past M (N) and K blocks past K with zeros instead of reading the padding.
@@ -209,14 +215,18 @@ inline size_t rbuf_bytes() { return (size_t)num_sms() * kBM * kBN * sizeof(long 
 
 // Largest K (a multiple of kKStep) one pass may sum without the int64
 // accumulator overflowing 2^62 for S slices.
-inline int64_t max_k_per_pass(int S) {
-    // |R| <= K * 2^14 * sum_d (d+1) 2^(8 (S-1-d))
+// Largest K (a multiple of kKStep) for which the exact sum over slice groups
+// d0 <= d < d1, R = sum_d 2^(8 (d1-1-d)) G_d, stays below 2^62 in magnitude:
+// |G_d| <= (d+1) K 2^14.
+inline int64_t max_k_per_pass_groups(int d0, int d1) {
     double w = 0.0;
-    for (int d = 0; d < S; d++) w += (d + 1) * std::ldexp(1.0, 8 * (S - 1 - d));
+    for (int d = d0; d < d1; d++) w += (d + 1) * std::ldexp(1.0, 8 * (d1 - 1 - d));
     double kmax = std::ldexp(1.0, 62) / (std::ldexp(1.0, 14) * w);
-    int64_t k = (int64_t)kmax;
+    int64_t k = kmax > 9.0e18 ? INT64_MAX : (int64_t)kmax;
     return (k / kKStep) * kKStep;
 }
+
+inline int64_t max_k_per_pass(int S) { return max_k_per_pass_groups(0, S); }
 
 // A-priori bound on the relative error of one product, relative to
 // sum_k |A_row| |B_col| scaled to the row maxima: the dropped digit tail of

@@ -296,7 +296,6 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     const int total_tiles =
         GROUPED ? ntiles_total : p.nbatch * ((p.mtiles + CL - 1) / CL) * p.ntiles * p.ksplit;
-    const int S = p.S;
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
@@ -324,7 +323,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                         ptx::tma_prefetch_desc(mB);
                     }
                 }
-                for (int d = 0; d < S && ok; d++) {
+                for (int d = p.d0; d < p.d1 && ok; d++) {
                     for (int s = 0; s <= d && ok; s++) {
                         const int t = d - s;
                         for (int kb = 0; kb < job.nkb; kb += GROUP_KB) {
@@ -398,7 +397,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             uint32_t dt = tmem;
             // Position in the group sequence: tile, slice group d, pair s, group g
             // of the pair (gpp groups per pair), groups in the open chunk.
-            int tile = cta0, d = 0, s = 0, g = 0, in_chunk = 0;
+            int tile = cta0, d = p.d0, s = 0, g = 0, in_chunk = 0;
             int gpp = tile < total_tiles ? entry_nkb<GROUPED>(p, items, work, tile) / GROUP_KB : 0;
             auto close_chunk = [&]() {
                 commit(&accf[abuf]);
@@ -440,8 +439,8 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (++s > d) {
                         s = 0;
                         if (in_chunk > 0) close_chunk(); // the slice group ends inside a chunk
-                        if (++d == S) {
-                            d = 0;
+                        if (++d == p.d1) {
+                            d = p.d0;
                             tile += ctas;
                             if (tile >= total_tiles) return false;
                             gpp = entry_nkb<GROUPED>(p, items, work, tile) / GROUP_KB;
@@ -600,7 +599,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int i = 0; i < kBN / 2; i++) L[i] = 0;
             bool hvalid = false; // H holds a part of the sum (else it reads as 0)
             int since_fold = 0;
-            for (int d = 0; d < S && ok; d++) {
+            for (int d = p.d0; d < p.d1 && ok; d++) {
                 const int kbs = (d + 1) * nkb;
                 for (int c0 = 0; c0 < kbs; c0 += kChunkKB) {
                     const long long tw = (p.prof && ew == 0 && lane == 0) ? clock64() : 0;
@@ -636,7 +635,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     // with the Horner step R *= 256 before the next one; after the last
                     // slice group H holds the tile's sums and L is free.
                     const bool group_end = c0 + kChunkKB >= kbs;
-                    const bool shift = group_end && d + 1 < S;
+                    const bool shift = group_end && d + 1 < p.d1;
                     if (++since_fold == 64 || group_end) {
 #pragma unroll
                         for (int cc = 0; cc < kBN / 16; cc++) {

@@ -140,9 +140,26 @@ def test_rows_with_wide_dynamic_range(eg):
 
 
 def test_multi_pass_k_for_six_slices(eg):
-    # six slices sum at most 192 terms per pass, so K=700 takes four passes
+    # six slices' exact sum fits int64 only up to K = 128; K = 700 runs slice
+    # groups 0-4 and 5 as two launches, each over the whole K
     err, _ = run_case(eg, "ij", "ik", "kj", {"i": 100, "j": 100, "k": 700}, cp=0.3, ab=2.0, slices=6)
     assert err < 1e-12, err
+
+
+@pytest.mark.parametrize("S,K", [(6, 1000), (6, 129), (5, 70000)])
+def test_slice_group_ranges_match_cpu_restatement(eg, S, K):
+    """When all slice groups' exact sum cannot take the whole K in int64, the groups
+    run as ranges (S = 6: 0-4 and 5), each range's exact sum rounded to FP64 and the
+    ranges added in order: bit for bit the CPU restatement of that plan."""
+    from test_split_math import split_product_ranges
+    rng = np.random.default_rng(S * K)
+    M, N = (37, 130) if K < 10000 else (9, 12)
+    A = rng.standard_normal((M, K)) * np.exp2(rng.integers(-8, 8, size=(M, 1)))
+    B = rng.standard_normal((N, K))
+    ref = split_product_ranges(A, B, S)
+    C = torch.full((M, N), np.nan, dtype=torch.float64, device="cuda")
+    eg.einsum(0.0, "ij", C, 1.0, "ik", cu(A), "jk", cu(B), precision="split_bf16", slices=S)
+    assert np.array_equal(C.cpu().numpy().view(np.uint64), ref.view(np.uint64))
 
 
 def test_nonfinite_row_gives_nan_row_only(eg):

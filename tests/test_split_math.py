@@ -67,6 +67,68 @@ def split_product_fast(A, B, S):
     return np.ldexp(R.astype(np.float64), shift.astype(np.int64))
 
 
+def max_k_per_pass_groups(d0, d1, kstep=128):
+    """Restates split.cuh max_k_per_pass_groups: the largest K (a multiple of 128)
+    for which sum_{d0 <= d < d1} 2^(8 (d1-1-d)) G_d stays below 2^62, |G_d| <= (d+1) K 2^14."""
+    w = sum((d + 1) * 2.0 ** (8 * (d1 - 1 - d)) for d in range(d0, d1))
+    k = int(2.0 ** 62 / (2.0 ** 14 * w))
+    return k // kstep * kstep
+
+
+def slice_group_ranges(S, Kp):
+    """Restates the launch plan of split.cu: greedy ranges of slice groups whose exact
+    sums fit int64 over the whole (padded) K."""
+    ranges, d0 = [], 0
+    while d0 < S:
+        d1 = d0 + 1
+        while d1 < S and max_k_per_pass_groups(d0, d1 + 1) >= Kp:
+            d1 += 1
+        ranges.append((d0, d1))
+        d0 = d1
+    return ranges
+
+
+def split_product_ranges(A, B, S):
+    """The split product as the GPU forms it when K needs several slice-group
+    ranges: each range's exact int64 sum rounded to FP64 on its own, the ranges
+    added in FP64 in order (the first stores, the others add)."""
+    K = A.shape[1]
+    assert K * 2 ** 14 < 2 ** 53
+    Kp = -(-K // 128) * 128
+    eA, eB = exponents(A), exponents(B)
+    a, b = digits(A, eA, S), digits(B, eB, S)
+    shift = (eA[:, None] + eB[None, :] - 2 * TOP - BITS * (S - 1)).astype(np.int64)
+    out = None
+    for d0, d1 in slice_group_ranges(S, Kp):
+        assert max_k_per_pass_groups(d0, d1) >= Kp
+        R = np.zeros((A.shape[0], B.shape[0]), dtype=np.int64)
+        for d in range(d0, d1):
+            G = sum(a[s].astype(np.float64) @ b[d - s].T.astype(np.float64) for s in range(d + 1))
+            R = R * 256 + G.astype(np.int64)
+        v = np.ldexp(R.astype(np.float64), shift + BITS * (S - d1))
+        out = v if out is None else out + v
+    return out
+
+
+def test_slice_group_ranges():
+    assert max_k_per_pass_groups(0, 5) == 65024
+    assert slice_group_ranges(5, 1024) == [(0, 5)]
+    assert slice_group_ranges(5, 65024) == [(0, 5)]
+    assert slice_group_ranges(5, 65152) == [(0, 4), (4, 5)]
+    assert max_k_per_pass_groups(0, 6) == 128
+    assert slice_group_ranges(6, 128) == [(0, 6)]
+    assert slice_group_ranges(6, 16384) == [(0, 5), (5, 6)]
+    assert slice_group_ranges(3, 1 << 20) == [(0, 3)]
+    rng = np.random.default_rng(8)
+    A, B = rng.standard_normal((7, 300)), rng.standard_normal((5, 300))
+    # one range: the same numbers as the single exact sum
+    assert np.array_equal(split_product_ranges(A, B, 5).view(np.uint64), split_product_fast(A, B, 5).view(np.uint64))
+    # two ranges for S = 6 and K = 300: within one FP64 rounding of the exact sum
+    two = split_product_ranges(A, B, 6)
+    assert slice_group_ranges(6, 384) == [(0, 5), (5, 6)]
+    assert np.allclose(two, split_product_fast(A, B, 6), rtol=4e-16, atol=0)
+
+
 def test_fast_split_product_matches_exact_integers():
     rng = np.random.default_rng(4)
     A = rng.standard_normal((9, 150)) * np.exp2(rng.integers(-30, 30, size=(9, 1)))
