@@ -569,18 +569,24 @@ def run_e2e(eg, T, precision, args, o, v, step_flops, chunks=8, return_outputs=F
     link = link_rates(host["g_vvvv"], out["Wabef"], [b for b, _ in slabs], rows_max, s_in, s_out)
     if world > 1:
         torch.distributed.barrier()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(s_in)
-    for i in range(steps):
-        step(i)
-    e1.record(s_out)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    ms = reduce_max_ms(e0.elapsed_time(e1) / steps, world, "cuda")
+    # Three passes of `steps` steps each; the reported time is the median pass.  The
+    # host link of this machine is shared, and single passes have been seen to take
+    # twice the link floor while the copy rates measured just before were normal.
+    passes = []
+    for _ in range(1 if precision == "fp64" else 3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s_in)
+        for i in range(steps):
+            step(i)
+        e1.record(s_out)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        passes.append(reduce_max_ms(e0.elapsed_time(e1) / steps, world, "cuda"))
+    ms = sorted(passes)[len(passes) // 2]
     floor_ms = (h2d + d2h) / (link["both_gbs"] * 1e9) * 1e3
     res = {"value": job_tflops(step_flops, ms, world), "unit": "TFLOP/s", "h2d_bytes_per_step": world * h2d,
-           "d2h_bytes_per_step": world * d2h, "ms_per_step": ms, "steps": steps,
+           "d2h_bytes_per_step": world * d2h, "ms_per_step": ms, "steps": steps, "passes_ms_per_step": passes,
            "link_gbs": link, "link_floor_ms": floor_ms, "frac_of_link_floor": floor_ms / ms,
            "pipelining": f"uploads, contractions and read-backs on three streams; three sets of the 0.6 GB inputs; "
                          f"Wabef in {chunks} slabs of rows a through four slab buffers"}
