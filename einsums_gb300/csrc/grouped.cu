@@ -35,6 +35,7 @@ eg_status lower_for_group(double cp, const int32_t *Cl, const eg_tensor *C, doub
                           const eg_tensor *A, const int32_t *Bl, const eg_tensor *B, const eg_options &opt,
                           Contraction &out, int32_t *alg_out, bool &gemm_shaped);
 eg_status encode_planes_public(CUtensorMap *map, void *base, int64_t Kp, int64_t rows, int64_t planes);
+int64_t mode_group_affine_stride(const ModeGroup &g, int comp);
 eg_status encode_planes_extent(CUtensorMap *map, void *base, int64_t K, int64_t rows, int64_t planes, int64_t Kp,
                                int64_t Rp);
 void set_capture_mode(bool on);
@@ -167,6 +168,7 @@ struct GOp {
     int64_t rowbase;      // first entry in the row-max / exponent arrays
     int64_t zbase;        // first digit plane
     int64_t rtab, ktab;   // first entries of this operand's row and K offsets in the plan's offset table
+    int64_t sr, sk;       // the single element stride of the rows / of K when the modes nest (else 0: tables)
 };
 
 __device__ __forceinline__ int64_t pick(int comp, int64_t oa, int64_t ob) { return comp == 0 ? oa : ob; }
@@ -196,6 +198,8 @@ __global__ void __launch_bounds__(kGThreads, 4) k_grouped_split(const GOp *ops, 
         const int64_t K = g.K;
         const int nr = (int)(g.rows - r0 < kGU ? g.rows - r0 : kGU);
         const long long *koff = offs + g.ktab; // element offset of each k in this operand
+        const int64_t sk = g.sk;
+        auto kofs = [&](int64_t k) -> int64_t { return sk ? k * sk : (int64_t)__ldg(koff + k); };
         const double *X = g.X;
         int64_t oa, ob, oc;
         group_offsets(g.bg, b, oa, ob, oc);
@@ -206,7 +210,9 @@ __global__ void __launch_bounds__(kGThreads, 4) k_grouped_split(const GOp *ops, 
 #pragma unroll
         for (int j = 0; j < kGU / kGWarps; j++) {
             const int rr = row_fast ? lane : w + kGWarps * j;
-            orow[j] = (rr < nr && (j == 0 || !row_fast)) ? obase + __ldg(offs + g.rtab + r0 + rr) : 0;
+            orow[j] = (rr < nr && (j == 0 || !row_fast))
+                          ? obase + (g.sr ? (r0 + rr) * g.sr : (int64_t)__ldg(offs + g.rtab + r0 + rr))
+                          : 0;
         }
         // phase 1: row maxima of |x| as IEEE bit patterns
         if (row_fast) {
@@ -214,7 +220,7 @@ __global__ void __launch_bounds__(kGThreads, 4) k_grouped_split(const GOp *ops, 
             if (lane < nr) {
 #pragma unroll 8
                 for (int64_t k = w; k < K; k += kGWarps)
-                    mx = max(mx, split::abs_bits(__ldg(X + orow[0] + __ldg(koff + k))));
+                    mx = max(mx, split::abs_bits(__ldg(X + orow[0] + kofs(k))));
             }
             red[w][lane] = mx;
         } else {
@@ -225,7 +231,7 @@ __global__ void __launch_bounds__(kGThreads, 4) k_grouped_split(const GOp *ops, 
                 if (rr < nr) {
 #pragma unroll 4
                     for (int64_t k = lane; k < K; k += 32)
-                        mx = max(mx, split::abs_bits(__ldg(X + orow[j] + __ldg(koff + k))));
+                        mx = max(mx, split::abs_bits(__ldg(X + orow[j] + kofs(k))));
                 }
                 for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
                 if (lane == 0) {
@@ -256,7 +262,7 @@ __global__ void __launch_bounds__(kGThreads, 4) k_grouped_split(const GOp *ops, 
 #pragma unroll
                 for (int kk = w; kk < kGK; kk += kGWarps) {
                     const int64_t k = k0 + kk;
-                    tile[lane][kk] = (k < K && lane < nr) ? __ldg(X + orow[0] + __ldg(koff + k)) : 0.0;
+                    tile[lane][kk] = (k < K && lane < nr) ? __ldg(X + orow[0] + kofs(k)) : 0.0;
                 }
             } else {
 #pragma unroll
@@ -265,7 +271,7 @@ __global__ void __launch_bounds__(kGThreads, 4) k_grouped_split(const GOp *ops, 
 #pragma unroll
                     for (int h = 0; h < kGK / 32; h++) {
                         const int64_t k = k0 + lane + 32 * h;
-                        tile[rr][lane + 32 * h] = (rr < nr && k < K) ? __ldg(X + orow[j] + __ldg(koff + k)) : 0.0;
+                        tile[rr][lane + 32 * h] = (rr < nr && k < K) ? __ldg(X + orow[j] + kofs(k)) : 0.0;
                     }
                 }
             }
@@ -548,6 +554,8 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
         a.Kp = Kp;
         a.rowbase = rowsA;
         a.zbase = zA;
+        a.sr = mode_group_affine_stride(c.m, 0);
+        a.sk = mode_group_affine_stride(c.k, 0);
         GOp b = a;
         b.X = c.B;
         b.rg = c.n;
@@ -557,6 +565,8 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
         b.Rp = Np;
         b.rowbase = rowsB;
         b.zbase = zB;
+        b.sr = mode_group_affine_stride(c.n, 1);
+        b.sk = mode_group_affine_stride(c.k, 1);
         opsA.push_back(a);
         opsB.push_back(b);
         TcItem it{};

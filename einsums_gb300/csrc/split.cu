@@ -364,6 +364,8 @@ eg_status encode_planes_public(CUtensorMap *map, void *base, int64_t Kp, int64_t
     return split::encode_planes(map, base, Kp, rows, planes);
 }
 
+int64_t mode_group_affine_stride(const ModeGroup &g, int comp) { return split::affine_stride(g, comp); }
+
 // A tiled map over an FP64 tensor of rank 2..5: dims[0] is the contiguous mode,
 // strides_bytes[i] the byte stride of mode i + 1, no swizzle, zero fill.
 eg_status encode_tiled_f64(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
