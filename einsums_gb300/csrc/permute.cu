@@ -152,6 +152,7 @@ constexpr int kTmaTile = 32, kTmaStages = 4, kTmaThreads = 256;
 constexpr int kTmaBoxBytes = kTmaTile * kTmaTile * 8;
 constexpr int kTmaSmem = 2 * kTmaStages * kTmaBoxBytes + 128 + 1024;
 constexpr unsigned long long kTmaWaitNs = 2000ull * 1000 * 1000;
+constexpr unsigned long long kTmaDrainNs = 200ull * 1000 * 1000;
 
 struct TmaPermute {
     int rank = 0;                  // tensor-map rank: 2 + rest modes (at most 5)
@@ -257,7 +258,8 @@ __global__ void __launch_bounds__(kTmaThreads) k_permute_tma(const __grid_consta
     if (tid == 0)
         for (uint32_t k = 0; k < kTmaStages; k++) issue_load(k);
     int st_c[5] = {0, 0, 0, 0, 0}; // thread 0: the store coordinates of the current tile
-    for (uint32_t k = 0; first + k * step < tp.total; k++) {
+    uint32_t k = 0;
+    for (; first + k * step < tp.total; k++) {
         const int slot = (int)(k % kTmaStages);
         const uint32_t parity = (k / kTmaStages) & 1u;
         if (tid == 0) {
@@ -292,6 +294,12 @@ __global__ void __launch_bounds__(kTmaThreads) k_permute_tma(const __grid_consta
         }
     }
     if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    if (*abort_flag && tid == 0) {
+        // a wait gave up at tile k: the loads of tiles k .. k + stages - 1 may still be
+        // in flight into this CTA's shared memory; give each a bounded wait to land
+        for (uint32_t kk = k; kk < k + kTmaStages && first + kk * step < tp.total; kk++)
+            ptx::mbar_wait(&full[kk % kTmaStages], (kk / kTmaStages) & 1u, kTmaDrainNs, nullptr);
+    }
     __syncthreads();
 }
 

@@ -741,54 +741,129 @@ __global__ void __launch_bounds__(THREADS, 1)
                 // the same conversion and stores as finalize_cols, the sums read from TMEM
                 const bool rows_fast = job.mg->n > 0 && job.mg->s[2][job.mg->n - 1] == 1;
                 double *const Cj = job.C;
+                if constexpr (GROUPED) {
+                    // grouped tiles (mostly partial, written once with C_prefactor 0): one
+                    // column at a time measured faster than loading C ahead
 #pragma unroll 1
-                for (int cc = 0; cc < kBN / 32; cc++) {
-                    uint32_t lo[16], hi[16];
-                    ptx::tmem_ld16(tl + 256u + (uint32_t)(col0 + cc * 16), lo);
-                    ptx::tmem_ld16(tl + 384u + (uint32_t)(col0 + cc * 16), hi);
-                    ptx::tmem_wait_ld();
+                    for (int cc = 0; cc < kBN / 32; cc++) {
+                        uint32_t lo[16], hi[16];
+                        ptx::tmem_ld16(tl + 256u + (uint32_t)(col0 + cc * 16), lo);
+                        ptx::tmem_ld16(tl + 384u + (uint32_t)(col0 + cc * 16), hi);
+                        ptx::tmem_wait_ld();
 #pragma unroll
-                    for (int b = 0; b < 16; b += kFinCols) {
-                        const int c0 = cc * 16 + b;
-                        double v[kFinCols];
+                        for (int b = 0; b < 16; b += kFinCols) {
+                            const int c0 = cc * 16 + b;
+                            double v[kFinCols];
 #pragma unroll
-                        for (int i = 0; i < kFinCols; i++) {
-                            const int ce = colExp[c0 + i];
-                            v[i] = 0.0;
-                            if (row_ok && ce != INT_MAX) {
-                                long long R = (long long)(((unsigned long long)hi[b + i] << 32) | lo[b + i]);
-                                if (p.ab_neg) R = -R;
-                                if (rowExp == INT_MIN || ce == INT_MIN)
-                                    v[i] = __longlong_as_double(0x7ff8000000000000ll);
-                                else
-                                    v[i] = int_times_pow2_rn(R, rowExp + ce + p.shift_const);
-                                if (!p.ab_pow2) v[i] *= p.ab;
+                            for (int i = 0; i < kFinCols; i++) {
+                                const int ce = colExp[c0 + i];
+                                v[i] = 0.0;
+                                if (row_ok && ce != INT_MAX) {
+                                    long long R = (long long)(((unsigned long long)hi[b + i] << 32) | lo[b + i]);
+                                    if (p.ab_neg) R = -R;
+                                    if (rowExp == INT_MIN || ce == INT_MIN)
+                                        v[i] = __longlong_as_double(0x7ff8000000000000ll);
+                                    else
+                                        v[i] = int_times_pow2_rn(R, rowExp + ce + p.shift_const);
+                                    if (!p.ab_pow2) v[i] *= p.ab;
+                                }
+                            }
+                            if (rows_fast) {
+                                if (row_ok) {
+#pragma unroll
+                                    for (int i = 0; i < kFinCols; i++) {
+                                        if (colExp[c0 + i] == INT_MAX) continue;
+                                        double *const cp_ = Cj + rowOff + colOff[c0 + i];
+                                        *cp_ = plain_store ? v[i] : (cp_one ? *cp_ + v[i] : fma(p.cp, *cp_, v[i]));
+                                    }
+                                }
+                            } else {
+#pragma unroll
+                                for (int i = 0; i < kFinCols; i++) finT[i * FIN_T + lane] = v[i];
+                                __syncwarp();
+                                // lanes kFinCols*r .. kFinCols*r + kFinCols-1 take the batch's columns of row r
+#pragma unroll
+                                for (int k = 0; k < kFinCols; k++) {
+                                    const int e = k * 32 + lane, r = e / kFinCols, c = e % kFinCols;
+                                    if (rowOkW[r] && colExp[c0 + c] != INT_MAX) {
+                                        const double w = finT[c * FIN_T + r];
+                                        double *const cp_ = Cj + rowOffW[r] + colOff[c0 + c];
+                                        *cp_ = plain_store ? w : (cp_one ? *cp_ + w : fma(p.cp, *cp_, w));
+                                    }
+                                }
+                                __syncwarp();
                             }
                         }
-                        if (rows_fast) {
-                            if (row_ok) {
+                    }
+                } else {
+#pragma unroll 1
+                    for (int cc = 0; cc < kBN / 32; cc++) {
+                        // per batch, C's old values are loaded first, all at once (a load after
+                        // each store would wait a full memory round trip per column, since the
+                        // stores may alias later loads), then converted sums are added and stored
+                        constexpr int NB = 16 / kFinCols; // batches per block
+                        uint32_t lo[16], hi[16];
+                        ptx::tmem_ld16(tl + 256u + (uint32_t)(col0 + cc * 16), lo);
+                        ptx::tmem_ld16(tl + 384u + (uint32_t)(col0 + cc * 16), hi);
+                        ptx::tmem_wait_ld();
+#pragma unroll
+                        for (int bb = 0; bb < NB; bb++) {
+                            const int b = bb * kFinCols;
+                            const int c0 = cc * 16 + b;
+                            double old[kFinCols];
+#pragma unroll
+                            for (int i = 0; i < kFinCols; i++) old[i] = 0.0;
+                            if (!plain_store) {
 #pragma unroll
                                 for (int i = 0; i < kFinCols; i++) {
-                                    if (colExp[c0 + i] == INT_MAX) continue;
-                                    double *const cp_ = Cj + rowOff + colOff[c0 + i];
-                                    *cp_ = plain_store ? v[i] : (cp_one ? *cp_ + v[i] : fma(p.cp, *cp_, v[i]));
+                                    if (rows_fast) {
+                                        if (row_ok && colExp[c0 + i] != INT_MAX) old[i] = Cj[rowOff + colOff[c0 + i]];
+                                    } else {
+                                        // lanes kFinCols*r .. kFinCols*r + kFinCols-1 take the batch's columns of row r
+                                        const int e = i * 32 + lane, r = e / kFinCols, c = e % kFinCols;
+                                        if (rowOkW[r] && colExp[c0 + c] != INT_MAX) old[i] = Cj[rowOffW[r] + colOff[c0 + c]];
+                                    }
                                 }
                             }
-                        } else {
+                            double v[kFinCols];
 #pragma unroll
-                            for (int i = 0; i < kFinCols; i++) finT[i * FIN_T + lane] = v[i];
-                            __syncwarp();
-                            // lanes kFinCols*r .. kFinCols*r + kFinCols-1 take the batch's columns of row r
-#pragma unroll
-                            for (int k = 0; k < kFinCols; k++) {
-                                const int e = k * 32 + lane, r = e / kFinCols, c = e % kFinCols;
-                                if (rowOkW[r] && colExp[c0 + c] != INT_MAX) {
-                                    const double w = finT[c * FIN_T + r];
-                                    double *const cp_ = Cj + rowOffW[r] + colOff[c0 + c];
-                                    *cp_ = plain_store ? w : (cp_one ? *cp_ + w : fma(p.cp, *cp_, w));
+                            for (int i = 0; i < kFinCols; i++) {
+                                const int ce = colExp[c0 + i];
+                                v[i] = 0.0;
+                                if (row_ok && ce != INT_MAX) {
+                                    long long R = (long long)(((unsigned long long)hi[b + i] << 32) | lo[b + i]);
+                                    if (p.ab_neg) R = -R;
+                                    if (rowExp == INT_MIN || ce == INT_MIN)
+                                        v[i] = __longlong_as_double(0x7ff8000000000000ll);
+                                    else
+                                        v[i] = int_times_pow2_rn(R, rowExp + ce + p.shift_const);
+                                    if (!p.ab_pow2) v[i] *= p.ab;
                                 }
                             }
-                            __syncwarp();
+                            if (rows_fast) {
+                                if (row_ok) {
+#pragma unroll
+                                    for (int i = 0; i < kFinCols; i++) {
+                                        if (colExp[c0 + i] == INT_MAX) continue;
+                                        Cj[rowOff + colOff[c0 + i]] =
+                                            plain_store ? v[i] : (cp_one ? old[i] + v[i] : fma(p.cp, old[i], v[i]));
+                                    }
+                                }
+                            } else {
+#pragma unroll
+                                for (int i = 0; i < kFinCols; i++) finT[i * FIN_T + lane] = v[i];
+                                __syncwarp();
+#pragma unroll
+                                for (int k = 0; k < kFinCols; k++) {
+                                    const int e = k * 32 + lane, r = e / kFinCols, c = e % kFinCols;
+                                    if (rowOkW[r] && colExp[c0 + c] != INT_MAX) {
+                                        const double w = finT[c * FIN_T + r];
+                                        Cj[rowOffW[r] + colOff[c0 + c]] =
+                                            plain_store ? w : (cp_one ? old[k] + w : fma(p.cp, old[k], w));
+                                    }
+                                }
+                                __syncwarp();
+                            }
                         }
                     }
                 }
