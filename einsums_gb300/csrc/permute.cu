@@ -506,6 +506,7 @@ eg_status run_permute(const PermuteLaunch &pl, const double *A, double *C, cudaS
     if (pl.tma) {
         const eg_status st = run_permute_tma(pl, A, C, s);
         if (st != EG_ERROR_NOT_SUPPORTED) return st;
+        set_error(""); // the tile kernel below takes the case the TMA form declined
     }
     if (pl.rows) {
         {
