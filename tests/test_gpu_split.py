@@ -241,7 +241,9 @@ def pair_cases():
 def test_single_cta_tiles_are_the_exact_split_product(eg):
     """Outputs of several 128-row tiles, odd tile counts and a K cut into slices
     (260 x 100, K = 2048): bit for bit the CPU restatement of the scheme."""
-    assert pair_cases() == 0  # this process runs single-CTA tiles
+    clusters = pair_cases()
+    if os.environ.get("EINSUMS_GB300_TC_PAIRS") != "1":
+        assert clusters == 0  # this process runs single-CTA tiles
 
 
 def test_pair_tiles_are_the_exact_split_product(eg):
