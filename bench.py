@@ -421,7 +421,7 @@ def run_ours(args, rank, world):
                 # through L2 by the output tiles that share them).
                 roof["traffic"] = TC_TRAFFIC_O32_V160
                 roof["traffic_unit"] = ("bytes per launch, mean of the step's 3 launches, from an ncu capture of "
-                                        "this workload (profiles/k_tc_split_gemm_traffic_ccd_o32_v160.md), "
+                                        "this workload (dram__bytes_read.sum + dram__bytes_write.sum), "
                                         "not measured in this run")
                 roof["algorithmic_bytes"] = tc_algorithmic_bytes(o, v, 5)
         else:
