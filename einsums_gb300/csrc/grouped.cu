@@ -648,6 +648,7 @@ eg_status build_split_plan(Plan &plan, const std::vector<Contraction> &cs, int s
     for (size_t i = 0; i < items.size(); i++) {
         const TcItem &it = items[i];
         const Contraction &c = cs[i];
+        if (it.M == 0 || it.N == 0 || c.batch.total == 0) continue; // no tiles: the maps are never used
         const int64_t planes = c.batch.total * S, K = c.k.total;
         const size_t plane = (size_t)Rmax * Kmaxp;
         if ((st = encode_planes_extent(&maps[2 * i], (__nv_bfloat16 *)planesA + (size_t)it.zA * plane, K, it.M, planes,

@@ -126,3 +126,29 @@ def test_grouped_split_operand_layouts(eg, pattern):
             oracle.einsum(Cl, ref, 0.5, 2.0, Al, As[k], Bl, Bs[k])
             assert oracle.rel_fro(tC[k].cpu().numpy(), ref) < 1e-10, k
     plan.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split_bf16"])
+def test_list_einsum_with_empty_items(eg, precision):
+    """A list with empty items (an output extent 0): a grouped plan refuses it, and
+    the list form of execute runs the items one by one with the other items'
+    results correct."""
+    rng = np.random.default_rng(17)
+    shapes = [(3, 4, 20, 30), (3, 4, 0, 10), (2, 5, 12, 0), (6, 7, 33, 41)]
+    As = [rng.standard_normal((i, j, a)) for i, j, a, b in shapes]
+    Bs = [rng.standard_normal((i, j, b)) for i, j, a, b in shapes]
+    Cs = [rng.standard_normal((a, b)) for i, j, a, b in shapes]
+    from einsums_gb300 import _lib
+    with pytest.raises(_lib.NotSupportedError):
+        eg.GroupedPlan(0.5, "ab", [cu(c) for c in Cs], -1.25, "ija", [cu(a) for a in As], "ijb",
+                       [cu(b) for b in Bs], precision=precision)
+    tC = [cu(c) for c in Cs]
+    eg.compile_plan("ab", "ija", "ijb").execute(0.5, tC, -1.25, [cu(a) for a in As], [cu(b) for b in Bs],
+                                                 precision=precision)
+    torch.cuda.synchronize()
+    tol = 1e-12 if precision == "fp64" else 1e-10
+    for a, b, c0, c in zip(As, Bs, Cs, tC):
+        ref = c0.copy()
+        oracle.einsum("ab", ref, 0.5, -1.25, "ija", a, "ijb", b)
+        if ref.size:
+            assert oracle.rel_fro(c.cpu().numpy(), ref) < tol
