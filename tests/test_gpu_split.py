@@ -233,6 +233,16 @@ def pair_cases():
         Ct = torch.zeros((N, M), dtype=torch.float64, device="cuda")
         eg.einsum(0.0, "ji", Ct, 1.0, "ik", cu(A), "jk", cu(B), precision="split_bf16", slices=5)
         assert np.array_equal(Ct.cpu().numpy().T.copy().view(np.uint64), ref.view(np.uint64)), (M, N, K, "rows")
+    # a batch index: each batch's tiles are scheduled as their own pairs
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((2, 300, 192))
+    B = rng.standard_normal((2, 140, 192))
+    C = torch.zeros((2, 300, 140), dtype=torch.float64, device="cuda")
+    eg.einsum(0.0, "bij", C, 1.0, "bik", cu(A), "bjk", cu(B), precision="split_bf16", slices=5)
+    got = C.cpu().numpy()
+    for b in range(2):
+        want = split_product_fast(A[b], B[b], 5)
+        assert np.array_equal(got[b].view(np.uint64), want.view(np.uint64)), ("batch", b)
     n = ctypes.c_int32(-1)
     _lib.check(_lib.load().eg_tc_pair_clusters(ctypes.byref(n)))
     return n.value
