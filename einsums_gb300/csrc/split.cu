@@ -4,9 +4,10 @@
 //                    pattern of |x|, which orders like the value; deterministic)
 //   k_split_exponent row exponent e with |x| < 2^e (INT_MIN for a row holding
 //                    Inf/NaN, whose outputs are written as NaN)
-//   k_split_digits   32x32 tiles staged through shared memory so the operand is
-//                    read along its contiguous mode and the digit planes are
-//                    written along k; padding rows/columns are written as 0
+//   k_split_digits   32x64 tiles staged through shared memory (double-buffered
+//                    asynchronous copies) so the operand is read along its
+//                    contiguous mode and the digit planes are written along k;
+//                    padding rows/columns are written as 0
 // then the tcgen05 GEMM (tc_gemm.cu) over the digit planes.  The operands'
 // index permutation is folded into the address maps of these kernels and of
 // the GEMM epilogue: nothing but the BF16 digit planes is materialised.
@@ -54,6 +55,7 @@ struct OperandMap {
 __device__ __forceinline__ int64_t comp_of(int comp, int64_t oa, int64_t ob) { return comp == 0 ? oa : ob; }
 
 __device__ __forceinline__ int64_t off_b(const OperandMap &m, int64_t b) {
+    if (m.bg.n == 0) return 0;
     int64_t oa, ob, oc;
     group_offsets(m.bg, b, oa, ob, oc);
     return comp_of(m.comp, oa, ob);
@@ -86,38 +88,67 @@ __global__ void k_operand_offsets(OperandMap m, int64_t *offr, int64_t *offk) {
 
 constexpr int T = 32, TR = 8;
 
-// Work units of 32 rows x kchunk k (kchunk a multiple of T), the k loop inside
-// the unit so that the unit's decomposition, batch offset and row offsets are
-// paid once per unit; one atomicMax per row per unit.  row_fast: the operand is
-// contiguous along rows (lanes walk rows), else along k (lanes walk k).
+// Splits a work index w = (b * n1 + i1) * n0 + i0 into its parts, in 32-bit
+// arithmetic when the work count fits (`narrow`): a 64-bit division is a long
+// subroutine, and the splitting kernels pay this once per work unit.
+__device__ __forceinline__ void split_unit(int64_t w, int64_t n0, int64_t n1, bool narrow, int64_t &i0, int64_t &i1,
+                                           int64_t &b) {
+    if (narrow) {
+        const uint32_t x = (uint32_t)w, a = (uint32_t)n0, c = (uint32_t)n1;
+        const uint32_t q = x / a, q2 = q / c;
+        i0 = x - q * a;
+        i1 = q - q2 * c;
+        b = q2;
+    } else {
+        const int64_t q = w / n0, q2 = q / n1;
+        i0 = w - q * n0;
+        i1 = q - q2 * n1;
+        b = q2;
+    }
+}
+
+// Row maxima over work units of rows x kchunk k (kchunk a multiple of T), the
+// k loop inside the unit so that the unit's decomposition, batch offset and
+// row offsets are paid once per unit; one atomicMax per row per unit.
+//
+// row_fast (the operand is contiguous along rows): a unit is 256 rows, one per
+// thread, each thread walking all k of the chunk for its row with 8 loads in
+// flight.  A CTA's eight warps read 2 KB contiguous at each k, and consecutive
+// units are consecutive row blocks at the same k range; no reduction between
+// threads is needed.  Otherwise (contiguous along k): a unit is 32 rows, lanes
+// walk k and each warp reduces its 4 rows with shuffles at the unit's end.
+constexpr int kRowFastBatch = 8;   // loads a thread keeps in flight when it walks one row
+constexpr int kRowFastRows = T * TR; // rows of a unit when the operand is contiguous along rows
 __global__ void __launch_bounds__(T *TR, 5) k_split_rowmax(OperandMap m, const double *__restrict__ X,
                                                         unsigned long long *rowmax, int row_fast, int kchunk) {
-    __shared__ unsigned long long red[TR][T];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int64_t rt = (m.rows + T - 1) / T, kcs = (m.K + kchunk - 1) / kchunk;
+    const int64_t rows_per_unit = row_fast ? kRowFastRows : T;
+    const int64_t rt = (m.rows + rows_per_unit - 1) / rows_per_unit, kcs = (m.K + kchunk - 1) / kchunk;
     const int64_t units = (int64_t)m.nbatch * rt * kcs;
+    const bool narrow = units < INT_MAX;
     for (int64_t u = blockIdx.x; u < units; u += gridDim.x) {
-        const int64_t kc = u % kcs, rtile = (u / kcs) % rt, b = u / (kcs * rt);
+        int64_t i0, i1, b;
+        split_unit(u, row_fast ? rt : kcs, row_fast ? kcs : rt, narrow, i0, i1, b);
+        const int64_t kc = row_fast ? i1 : i0, rtile = row_fast ? i0 : i1;
         const int64_t ob = off_b(m, b);
-        const int64_t r0 = rtile * T;
+        const int64_t r0 = rtile * rows_per_unit;
         const int64_t kbeg = kc * kchunk, kend = min(m.K, kbeg + kchunk);
         if (row_fast) {
-            // thread (tx, ty): row r0+tx, k = kbeg+ty, +8, ...
-            const int64_t r = r0 + tx;
-            unsigned long long mx = 0;
+            const int64_t r = r0 + ty * T + tx;
             if (r < m.rows) {
                 const double *xr = X + ob + off_r(m, r);
-#pragma unroll 4
-                for (int64_t k = kbeg + ty; k < kend; k += TR)
-                    mx = max(mx, abs_bits(__ldg(xr + off_k(m, k))));
+                unsigned long long mx = 0;
+                int64_t k = kbeg;
+                for (; k + kRowFastBatch <= kend; k += kRowFastBatch) {
+                    unsigned long long v[kRowFastBatch];
+#pragma unroll
+                    for (int i = 0; i < kRowFastBatch; i++) v[i] = abs_bits(__ldg(xr + off_k(m, k + i)));
+#pragma unroll
+                    for (int i = 0; i < kRowFastBatch; i++) mx = max(mx, v[i]);
+                }
+                for (; k < kend; k++) mx = max(mx, abs_bits(__ldg(xr + off_k(m, k))));
+                if (mx) atomicMax(rowmax + b * m.Rp + r, mx);
             }
-            red[ty][tx] = mx;
-            __syncthreads();
-            if (ty == 0) {
-                for (int j = 1; j < TR; j++) mx = max(mx, red[j][tx]);
-                if (r < m.rows && mx) atomicMax(rowmax + b * m.Rp + r, mx);
-            }
-            __syncthreads();
         } else {
             // thread (tx, ty): rows r0+ty, +8, ...; k = kbeg+tx, +32, ...; warp reduce along k
             constexpr int RPT = T / TR;
@@ -163,25 +194,41 @@ __global__ void k_split_exponent(const unsigned long long *rowmax, int *e, int64
 // read along its contiguous mode; each thread then converts two consecutive k
 // of a row and writes them as one BF16 pair per digit plane (a warp stores 128
 // contiguous bytes per plane).  Padding rows and columns are written as 0.
+//
+// A work unit is a strip of up to kDigitStrip k tiles of one 32-row tile, so
+// that the unit's decomposition, exponents and row offsets are paid per strip.
+// Consecutive units walk the operand's contiguous mode: k strips of one row
+// tile, or (row_fast) row tiles of one k strip.  Within a strip the tiles are
+// double-buffered: asynchronous copies (cp.async, zero-filled outside the
+// operand) bring tile t+1 into shared memory while tile t is converted.
 constexpr int TK = 2 * T;
 constexpr int64_t kDigitStrip = 8; // k tiles per work unit
+__device__ __forceinline__ void cp_async8(double *dst, const double *src, bool valid) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(src), "r"(valid ? 8 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 template <int S>
 __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const double *__restrict__ X, const int *rexp,
                                                         __nv_bfloat16 *planes, int row_fast) {
-    __shared__ double tile[T][TK + 1];
+    __shared__ double tile[2][T][TK + 1];
     __shared__ int ex[T];
     const int tx = threadIdx.x, ty = threadIdx.y;
-    // a work unit is a strip of up to kDigitStrip k tiles of one 32-row tile, so
-    // that the unit's decomposition, exponents and row offsets are paid per strip
     const int64_t rt = m.Rp / T, kt = m.Kp / TK, segs = (kt + kDigitStrip - 1) / kDigitStrip;
     const int64_t work = (int64_t)m.nbatch * rt * segs;
+    const bool narrow = work < INT_MAX;
     const int64_t plane = m.Rp * m.Kp;
     constexpr int RPT = T / TR;
     for (int64_t w = blockIdx.x; w < work; w += gridDim.x) {
-        const int64_t sg = w % segs, rtile = (w / segs) % rt, b = w / (segs * rt);
+        int64_t i0, i1, b;
+        split_unit(w, row_fast ? rt : segs, row_fast ? segs : rt, narrow, i0, i1, b);
+        const int64_t sg = row_fast ? i1 : i0, rtile = row_fast ? i0 : i1;
         const int64_t ob = off_b(m, b);
         const int64_t r0 = rtile * T;
-        __syncthreads(); // the previous strip's last reads of ex[] are done
+        __syncthreads(); // the previous strip's last reads of ex[] and of the tiles are done
         if (ty == 0) ex[tx] = (r0 + tx < m.rows) ? rexp[b * m.Rp + r0 + tx] : 0;
         const double *xr[RPT]; // row_fast: row r0+tx in xr[0]; else rows r0+ty+8j
 #pragma unroll
@@ -189,48 +236,62 @@ __global__ void __launch_bounds__(T *TR) k_split_digits(OperandMap m, const doub
             const int64_t r = row_fast ? (j == 0 ? r0 + tx : m.rows) : r0 + ty + TR * j;
             xr[j] = r < m.rows ? X + ob + off_r(m, r) : nullptr;
         }
-        const int64_t kt_end = min(kt, (sg + 1) * kDigitStrip);
-        for (int64_t ktile = sg * kDigitStrip; ktile < kt_end; ktile++) {
-        const int64_t k0 = ktile * TK;
-        if (row_fast) {
+        auto load_tile = [&](int buf, int64_t k0) {
+            if (row_fast) {
 #pragma unroll
-            for (int j = ty; j < TK; j += TR) {
-                const int64_t k = k0 + j;
-                tile[tx][j] = (xr[0] && k < m.K) ? __ldg(xr[0] + off_k(m, k)) : 0.0;
-            }
-        } else {
-#pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int64_t k = k0 + h * T + tx;
-                const bool kin = k < m.K;
-                const int64_t okk = kin ? off_k(m, k) : 0;
-#pragma unroll
-                for (int j = 0; j < RPT; j++) tile[ty + TR * j][h * T + tx] = (xr[j] && kin) ? __ldg(xr[j] + okk) : 0.0;
-            }
-        }
-        __syncthreads();
-        // write: thread tx converts k0 + 2tx and k0 + 2tx + 1 of each of its rows
-#pragma unroll
-        for (int j = ty; j < T; j += TR) {
-            const int64_t r = r0 + j;
-            uint32_t pk[S];
-            const int e = ex[j];
-            if (e == INT_MIN) {
-#pragma unroll
-                for (int s = 0; s < S; s++) pk[s] = 0u;
+                for (int j = ty; j < TK; j += TR) {
+                    const int64_t k = k0 + j;
+                    const bool ok = xr[0] && k < m.K;
+                    cp_async8(&tile[buf][tx][j], ok ? xr[0] + off_k(m, k) : X, ok);
+                }
             } else {
-                digits_bf16x2<S>(tile[j][2 * tx], tile[j][2 * tx + 1], e, pk);
-            }
-            uint32_t *out = (uint32_t *)(planes + ((int64_t)b * S) * plane + r * m.Kp + k0) + tx;
 #pragma unroll
-            for (int s = 0; s < S; s++) out[(int64_t)s * (plane / 2)] = pk[s];
-        }
-        __syncthreads();
+                for (int h = 0; h < 2; h++) {
+                    const int64_t k = k0 + h * T + tx;
+                    const bool kin = k < m.K;
+                    const int64_t okk = kin ? off_k(m, k) : 0;
+#pragma unroll
+                    for (int j = 0; j < RPT; j++) {
+                        const bool ok = xr[j] && kin;
+                        cp_async8(&tile[buf][ty + TR * j][h * T + tx], ok ? xr[j] + okk : X, ok);
+                    }
+                }
+            }
+            cp_async_commit();
+        };
+        const int64_t kt_beg = sg * kDigitStrip, kt_end = min(kt, (sg + 1) * kDigitStrip);
+        load_tile(0, kt_beg * TK);
+        for (int64_t ktile = kt_beg; ktile < kt_end; ktile++) {
+            const int cur = (int)((ktile - kt_beg) & 1);
+            const int64_t k0 = ktile * TK;
+            if (ktile + 1 < kt_end) {
+                load_tile(cur ^ 1, k0 + TK);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncthreads();
+            // write: thread tx converts k0 + 2tx and k0 + 2tx + 1 of each of its rows
+#pragma unroll
+            for (int j = ty; j < T; j += TR) {
+                const int64_t r = r0 + j;
+                uint32_t pk[S];
+                const int e = ex[j];
+                if (e == INT_MIN) {
+#pragma unroll
+                    for (int s = 0; s < S; s++) pk[s] = 0u;
+                } else {
+                    digits_bf16x2<S>(tile[cur][j][2 * tx], tile[cur][j][2 * tx + 1], e, pk);
+                }
+                uint32_t *out = (uint32_t *)(planes + ((int64_t)b * S) * plane + r * m.Kp + k0) + tx;
+#pragma unroll
+                for (int s = 0; s < S; s++) out[(int64_t)s * (plane / 2)] = pk[s];
+            }
+            __syncthreads();
         }
     }
 }
 
-// K chunk (a multiple of T) giving about eight work units per SM.
 // CTAs of `kernel` (256 threads, static shared memory) that fit on the GPU at
 // once: the splitting kernels launch exactly one wave of them and loop over
 // their work units, so no partial second wave trails the launch.
@@ -241,10 +302,26 @@ int resident_grid(F kernel) {
     return per_sm * num_sms();
 }
 
-// K chunk (a multiple of T) giving about `target` work units.
-int chunk_for(int64_t units_per_chunk_row, int64_t ktiles, int64_t target) {
-    const int64_t per_unit = std::max<int64_t>(1, (units_per_chunk_row * ktiles + target - 1) / target);
-    return (int)(std::min<int64_t>(per_unit, ktiles) * T);
+// K chunk (a multiple of `gran`) for `row_units` row blocks: among splits into
+// about one to four units per resident CTA, the one whose last wave of units is
+// fullest (the fewest units when two are about as full).
+int balanced_chunk(int64_t row_units, int64_t K, int64_t resident, int gran) {
+    const int64_t ktiles = std::max<int64_t>(1, (K + gran - 1) / gran);
+    row_units = std::max<int64_t>(1, row_units);
+    int64_t best_tiles = ktiles;
+    double best_eff = -1.0;
+    for (int per = 1; per <= 4; per++) {
+        const int64_t want = std::min(ktiles, std::max<int64_t>(1, resident * per / row_units));
+        const int64_t tiles = (ktiles + want - 1) / want; // tiles of `gran` k per chunk
+        const int64_t units = row_units * ((ktiles + tiles - 1) / tiles);
+        const int64_t waves = (units + resident - 1) / resident;
+        const double eff = (double)units / (double)(waves * resident);
+        if (eff > best_eff + 0.02) {
+            best_eff = eff;
+            best_tiles = tiles;
+        }
+    }
+    return (int)(best_tiles * gran);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -321,9 +398,9 @@ eg_status split_operand(OperandMap om, const double *X, unsigned long long *rowm
     const int cap = num_sms() * 8;
     {
         static const int resident = resident_grid(k_split_rowmax);
-        // about four units per resident CTA: one wave, balanced
-        const int64_t rows_units = (int64_t)om.nbatch * ((om.rows + T - 1) / T);
-        const int kchunk = chunk_for(rows_units, (om.K + T - 1) / T, 4 * (int64_t)resident);
+        const int64_t unit_rows = r_fast ? kRowFastRows : T;
+        const int64_t rows_units = (int64_t)om.nbatch * ((om.rows + unit_rows - 1) / unit_rows);
+        const int kchunk = balanced_chunk(rows_units, om.K, resident, r_fast ? kRowFastBatch : T);
         const int64_t work = rows_units * ((om.K + kchunk - 1) / kchunk);
         const int grid = (int)(work < resident ? (work < 1 ? 1 : work) : resident);
         LaunchScope ls_("k_split_rowmax", s);
