@@ -42,7 +42,7 @@ def flops(o, v):
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the tensor kernel on the
 # o=32, v=160 workload, mean over the step's three launches (Wmnij 3.32 GB,
 # Wabef 18.17 GB, Wmbej 6.37 GB), from a separate capture of this workload.
-TC_TRAFFIC_O32_V160 = 9.29e9
+TC_TRAFFIC_O32_V160 = 9.44e9
 
 
 def tc_algorithmic_bytes(o, v, S):
@@ -417,7 +417,7 @@ def run_ours(args, rank, world):
                 # launches, from one ncu capture of this workload
                 # (dram__bytes_read.sum + dram__bytes_write.sum); algorithmic bytes
                 # per launch (digit planes read once, C read and written once) are
-                # 4.16 GB; the kernel moves 2.2x that (digit-plane panels re-read
+                # 4.16 GB; the kernel moves 2.3x that (digit-plane panels re-read
                 # through L2 by the output tiles that share them).
                 roof["traffic"] = TC_TRAFFIC_O32_V160
                 roof["traffic_unit"] = ("bytes per launch, mean of the step's 3 launches, from an ncu capture of "
