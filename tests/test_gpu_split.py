@@ -300,3 +300,31 @@ def test_split_result_is_the_exact_split_product(eg, S, K):
     for a, b, c in zip(As, Bs, Cs):
         assert np.array_equal(c.cpu().numpy().view(np.uint64), split_product(a, b, S).view(np.uint64))
     plan.close()
+
+
+@pytest.mark.parametrize("layout", ["rows_contiguous", "k_contiguous"])
+def test_split_product_exact_for_both_operand_layouts(eg, layout):
+    """Row maxima and digits read operands stored either way round: rows
+    contiguous (A given as "bki", so the splitting kernels walk rows with k
+    strided) or k contiguous ("bik").  Row counts that are not a multiple of
+    the 256-row units, K not a multiple of the 8-load batches, two batches,
+    and rows spread over 2^-40 .. 2^40: bit for bit the CPU restatement."""
+    from test_split_math import split_product_fast
+    S, nb, M, N, K = 5, 2, 300, 37, 1003
+    rng = np.random.default_rng(7)
+    A = rng.standard_normal((nb, M, K)) * np.exp2(rng.integers(-40, 40, size=(nb, M, 1)))
+    B = rng.standard_normal((nb, N, K)) * np.exp2(rng.integers(-40, 40, size=(nb, N, 1)))
+    A[1, 299, :] = 0.0  # a zero row in the last, partial unit
+    if layout == "rows_contiguous":
+        Al, Bl = "bki", "bkj"
+        tA, tB = cu(A.transpose(0, 2, 1)), cu(B.transpose(0, 2, 1))
+    else:
+        Al, Bl = "bik", "bjk"
+        tA, tB = cu(A), cu(B)
+    C = torch.zeros((nb, M, N), dtype=torch.float64, device="cuda")
+    eg.einsum(0.0, "bij", C, 1.0, Al, tA, Bl, tB, precision="split_bf16", slices=S)
+    assert eg.last_split_report()["slices"] == S
+    got = C.cpu().numpy()
+    for b in range(nb):
+        ref = split_product_fast(A[b], B[b], S)
+        assert np.array_equal(got[b].view(np.uint64), ref.view(np.uint64)), b
