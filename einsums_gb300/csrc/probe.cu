@@ -13,8 +13,16 @@ namespace {
 
 constexpr int kChains = 8;
 
-__global__ void __launch_bounds__(256) k_probe_dfma(double *out, int iters, double seed, long long *cycles) {
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__global__ void __launch_bounds__(256) k_probe_dfma(double *out, int iters, double seed, long long *cycles,
+                                                    unsigned long long *ns) {
     const long long t0 = clock64();
+    const unsigned long long g0 = global_ns();
     double a[kChains];
 #pragma unroll
     for (int c = 0; c < kChains; c++) a[c] = seed + threadIdx.x * 1e-7 + c;
@@ -28,11 +36,16 @@ __global__ void __launch_bounds__(256) k_probe_dfma(double *out, int iters, doub
     for (int c = 0; c < kChains; c++) s += a[c];
     if (s == 1234.5) out[0] = s; // keeps the loop alive
     __syncthreads();
-    if (threadIdx.x == 0) cycles[blockIdx.x] = clock64() - t0;
+    if (threadIdx.x == 0) {
+        cycles[blockIdx.x] = clock64() - t0;
+        ns[blockIdx.x] = global_ns() - g0;
+    }
 }
 
-__global__ void __launch_bounds__(256) k_probe_dmma(double *out, int iters, double seed, long long *cycles) {
+__global__ void __launch_bounds__(256) k_probe_dmma(double *out, int iters, double seed, long long *cycles,
+                                                    unsigned long long *ns) {
     const long long t0 = clock64();
+    const unsigned long long g0 = global_ns();
     double acc[kChains][2];
 #pragma unroll
     for (int c = 0; c < kChains; c++) acc[c][0] = acc[c][1] = 0.0;
@@ -49,18 +62,25 @@ __global__ void __launch_bounds__(256) k_probe_dmma(double *out, int iters, doub
     for (int c = 0; c < kChains; c++) s += acc[c][0] + acc[c][1];
     if (s == 1234.5) out[0] = s;
     __syncthreads();
-    if (threadIdx.x == 0) cycles[blockIdx.x] = clock64() - t0;
+    if (threadIdx.x == 0) {
+        cycles[blockIdx.x] = clock64() - t0;
+        ns[blockIdx.x] = global_ns() - g0;
+    }
 }
 
 } // namespace
 } // namespace eg
 
 // flops: DFMA counts 2 per thread-FMA; m8n8k4 DMMA counts 2*8*8*4 per warp-instruction.
-// Best of three runs after a warm-up run.  Each block of the single resident
-// wave records its SM cycles; *probe_mhz (may be NULL) receives the clock the
-// DFMA loop ran at (its cycles over its event time) -- the dense FP64 loops run
-// well below the maximum SM clock on this GPU, so kernels that mix FP64 with
-// other work can exceed these rates.
+// Best of three runs after a warm-up run.  Each block records its SM cycles and
+// its own duration (global timer); *probe_mhz (may be NULL) receives the median
+// block's cycles over its duration, the SM clock the DFMA loop ran at.  Blocks
+// of one launch share the FP64 pipe unevenly and finish at different times, so
+// a block's cycles over the whole launch's time would understate the clock.
+// On GB300 both loops stay below the FP64 pipe's rate: ncu counts the DMMA
+// instructions on the FP64 pipe (none on the tensor pipe), at 97 % of its
+// active cycles, and the DFMA loop keeps the pipe 84 % busy, while the
+// register-tiled contraction kernel keeps it 96 % busy and runs faster.
 extern "C" eg_status eg_measure_fp64_peak(double *dfma_tflops, double *dmma_tflops) {
     return eg_measure_fp64_peak_clock(dfma_tflops, dmma_tflops, nullptr);
 }
@@ -74,15 +94,22 @@ extern "C" eg_status eg_measure_fp64_peak_clock(double *dfma_tflops, double *dmm
     EG_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev));
     double *d = nullptr;
     long long *cyc = nullptr;
+    unsigned long long *bns = nullptr;
     EG_CUDA(cudaMalloc(&d, sizeof(double)));
     if (cudaMalloc(&cyc, blocks * sizeof(long long)) != cudaSuccess) {
         cudaFree(d);
+        return fail(EG_ERROR_OUT_OF_MEMORY, "eg_measure_fp64_peak: cudaMalloc");
+    }
+    if (cudaMalloc(&bns, blocks * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaFree(d);
+        cudaFree(cyc);
         return fail(EG_ERROR_OUT_OF_MEMORY, "eg_measure_fp64_peak: cudaMalloc");
     }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     std::vector<long long> hc(blocks);
+    std::vector<unsigned long long> hn(blocks);
     // best of three runs after a warm-up run; returns the run's ms and its SM clock in MHz
     auto timed = [&](auto launch, double &mhz) -> float {
         float best = 1e30f;
@@ -94,23 +121,30 @@ extern "C" eg_status eg_measure_fp64_peak_clock(double *dfma_tflops, double *dmm
             cudaEventElapsedTime(&ms, e0, e1);
             if (rep > 0 && ms < best) {
                 best = ms;
-                if (cudaMemcpy(hc.data(), cyc, blocks * sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess)
+                if (cudaMemcpy(hc.data(), cyc, blocks * sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess ||
+                    cudaMemcpy(hn.data(), bns, blocks * sizeof(unsigned long long), cudaMemcpyDeviceToHost) !=
+                        cudaSuccess)
                     return -1.f;
-                std::vector<long long> sorted(hc);
-                std::sort(sorted.begin(), sorted.end());
-                mhz = (double)sorted[blocks / 2] / (ms * 1e3);
+                std::vector<double> clk;
+                clk.reserve(blocks);
+                for (int b = 0; b < blocks; b++)
+                    if (hn[b] > 0) clk.push_back((double)hc[b] * 1e3 / (double)hn[b]); // cycles per ns -> MHz
+                if (clk.empty()) return -1.f;
+                std::sort(clk.begin(), clk.end());
+                mhz = clk[clk.size() / 2];
             }
         }
         return best;
     };
     double mhz_fma = 0.0, mhz_mma = 0.0;
-    const float ms_fma = timed([&] { k_probe_dfma<<<blocks, threads>>>(d, iters, 1.0, cyc); }, mhz_fma);
-    const float ms_mma = timed([&] { k_probe_dmma<<<blocks, threads>>>(d, iters, 1.0, cyc); }, mhz_mma);
+    const float ms_fma = timed([&] { k_probe_dfma<<<blocks, threads>>>(d, iters, 1.0, cyc, bns); }, mhz_fma);
+    const float ms_mma = timed([&] { k_probe_dmma<<<blocks, threads>>>(d, iters, 1.0, cyc, bns); }, mhz_mma);
     const cudaError_t err = cudaGetLastError();
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(d);
     cudaFree(cyc);
+    cudaFree(bns);
     if (err != cudaSuccess) return cuda_fail(err, "eg_measure_fp64_peak");
     if (ms_fma <= 0.f || ms_mma <= 0.f || mhz_fma <= 0.0 || mhz_mma <= 0.0)
         return fail(EG_ERROR_CUDA, "eg_measure_fp64_peak: timing failed");

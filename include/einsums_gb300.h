@@ -283,8 +283,9 @@ eg_status eg_stream_synchronize(void *stream);
 /* Measures FP64 throughput of this device (TFLOP/s) with a DFMA loop and an
  * mma.sync m8n8k4 f64 (DMMA) loop (best of three runs after a warm-up run);
  * synchronises the device.  The roofline denominator of the plain FP64 form.
- * eg_measure_fp64_peak_clock also gives the SM clock (MHz) the DFMA loop ran at,
- * from its SM cycles over its duration.  No reference counterpart. */
+ * eg_measure_fp64_peak_clock also gives the SM clock (MHz) the DFMA loop ran at:
+ * each block's SM cycles over its own duration (global timer), median over the
+ * blocks.  No reference counterpart. */
 eg_status eg_measure_fp64_peak(double *dfma_tflops, double *dmma_tflops);
 eg_status eg_measure_fp64_peak_clock(double *dfma_tflops, double *dmma_tflops, double *probe_mhz);
 

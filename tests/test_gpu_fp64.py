@@ -287,3 +287,20 @@ def test_long_k_gemv_variants(eg, case):
     tC = cu(C0)
     eg.einsum(0.5, Cl, tC, -1.5, Al, cu(A), Bl, cu(B))
     assert oracle.rel_fro(tC.cpu().numpy(), ref) < TOL
+
+
+def test_fp64_probe_rates_and_clock(eg):
+    """The FP64 probes report positive rates and the SM clock the DFMA loop ran
+    at, from each block's cycles over its own duration: a plausible GB300 clock,
+    not the lower figure a block's cycles over the whole launch would give."""
+    import ctypes
+
+    from einsums_gb300 import _lib
+    lib = _lib.load()
+    dfma, dmma, mhz = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    _lib.check(lib.eg_measure_fp64_peak_clock(ctypes.byref(dfma), ctypes.byref(dmma), ctypes.byref(mhz)))
+    assert 0.1 < dfma.value < 5.0 and 0.1 < dmma.value < 5.0
+    assert 300.0 < mhz.value < 2300.0
+    # the DFMA loop cannot beat the FP64 pipe's rate, 4 flop per clock per SM
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    assert dfma.value <= 1.02 * 4.0 * sms * mhz.value * 1e6 / 1e12
