@@ -468,7 +468,8 @@ def run_ours(args, rank, world):
             "data": "synthetic (seeded torch generator on device; CCD amplitudes/integrals as specified)",
             "config": {"workload": f"CCD W intermediates o={o} v={v}: Wmnij, Wabef (GEMM), Wmbej (GENERIC), E (DOT)",
                        "precision": headline, "slices": (split_report or {}).get("slices"),
-                       "l2": "inputs larger than L2 (Wabef 5.24 GB read+written per step); no flush",
+                       "l2": f"inputs larger than L2 (Wabef {v ** 4 * 8 / 1e9:.2f} GB read+written per step); no flush"
+                       if v ** 4 * 8 > 129e6 else "inputs smaller than L2 (129 MB): a reduced case, not the headline",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "plain_fp64": {"value": fp64_value, "ms_per_step": ms_fp64, "per_contraction_ms": per_contraction_fp64,
                            "fp64_peak_tflops": fp64_peak, "dfma_tflops": dfma.value, "dmma_tflops": dmma.value,
